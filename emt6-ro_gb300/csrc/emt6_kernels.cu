@@ -1,0 +1,983 @@
+// emt6_kernels.cu -- sm_103a kernels of the EMT6-Ro batched simulation step.
+//
+// One CTA (192 threads) owns one simulation for a whole launch of N steps:
+// the three substrate fields (3 x 53 x 53 FP32), the site-state bytes and the
+// occupied list live in shared memory for the launch; per-site cell records
+// (48 B) stay in global memory, where the few hundred live cells of each
+// resident simulation stay L2-resident.  Per step (reference cadence,
+// src/emt6ro/simulation/simulation.cu:153-166):
+//   t % 128 == 0  rebuild the occupied list        (simulation.cu:41-64)
+//   t % 32  == 0  ROI + circular fixed-value mask   (diffusion.cu:65-100)
+//   diffusion: 23 substeps over free sites + 1 over the ROI (diffusion.cu:135-191).
+//     Each field is held in registers by a pair of warps (rows split in two
+//     halves; lane = column, or two columns for ROIs wider than 31); the
+//     horizontal neighbours come from warp shuffles, vertical ones from the
+//     same thread's registers, and the two halves swap one boundary row per
+//     substep through shared memory under a 64-thread named barrier.
+//   cell update: 8-neighbour vacancy snapshot, Site::step per list entry,
+//     at most one division per simulation (simulation.cu:66-110).
+// Randomness is Philox keyed by (step, simulation, site, occurrence), so the
+// results do not depend on the launch shape.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "emt6_device.cuh"
+#include "emt6_kernels.h"
+
+namespace emt6 {
+
+__device__ unsigned long long g_instr_counts[4];  // decisions, kills, irradiations, divisions
+__device__ double g_instr_sum_death_prob;
+__device__ unsigned long long g_instr_hist[600];  // irradiation bins, then time-in-repair
+
+struct Misc {
+  int roi[5];  // r0, c0, h, w, dist
+  uint32_t n, n0;
+  int has_multi;
+  int winner, target;
+  int red[12][4];
+  unsigned int ins[4];
+  double ins_dp;
+  unsigned long long diffused;
+  unsigned long long nfs;  // free sites of the current mask
+};
+
+__host__ __device__ inline uint32_t align_up(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
+
+struct SmemLayout {
+  uint32_t fld, st, list, aux, colmask, xch, misc, total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(int HW, int lcap, int np) {
+  SmemLayout L;
+  uint32_t o = 0;
+  // fld and st regions match the global per-simulation strides (3*HW padded
+  // to 32 floats, HW padded to 128 bytes) so whole-stride copies stay inside
+  L.fld = o; o += align_up(3u * (uint32_t)HW, 32) * 4u;
+  L.st = o; o += align_up((uint32_t)HW, 128);
+  L.list = o; o += align_up((uint32_t)lcap * 2u, 16);
+  L.aux = o; o += align_up((uint32_t)lcap, 16);
+  L.colmask = o; o += 64 * 8;
+  L.xch = o; o += 3u * (uint32_t)np * 128u * 16u;
+  L.misc = o; o += align_up(sizeof(Misc), 16);
+  L.total = o;
+  return L;
+}
+
+size_t run_kernel_smem(int HW, int lcap, bool wide) {
+  return smem_layout(HW, lcap, wide ? 4 : 2).total;
+}
+
+// ---------------------------------------------------------------------------
+// block reductions
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ __forceinline__ void block_minmax4(int v[4], Misc *m) {
+  // v = (min r, min c, max r, max c)
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    v[0] = min(v[0], __shfl_xor_sync(kFull, v[0], o));
+    v[1] = min(v[1], __shfl_xor_sync(kFull, v[1], o));
+    v[2] = max(v[2], __shfl_xor_sync(kFull, v[2], o));
+    v[3] = max(v[3], __shfl_xor_sync(kFull, v[3], o));
+  }
+  if (lane == 0)
+    for (int k = 0; k < 4; ++k) m->red[wid][k] = v[k];
+  __syncthreads();
+  v[0] = m->red[0][0]; v[1] = m->red[0][1]; v[2] = m->red[0][2]; v[3] = m->red[0][3];
+  for (int w = 1; w < NT / 32; ++w) {
+    v[0] = min(v[0], m->red[w][0]);
+    v[1] = min(v[1], m->red[w][1]);
+    v[2] = max(v[2], m->red[w][2]);
+    v[3] = max(v[3], m->red[w][3]);
+  }
+  __syncthreads();
+}
+
+template <int NT>
+__device__ __forceinline__ int block_max(int v, Misc *m) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
+  if (lane == 0) m->red[wid][0] = v;
+  __syncthreads();
+  v = m->red[0][0];
+  for (int w = 1; w < NT / 32; ++w) v = max(v, m->red[w][0]);
+  __syncthreads();
+  return v;
+}
+
+template <int NT>
+__device__ __forceinline__ int block_min(int v, Misc *m) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = min(v, __shfl_xor_sync(kFull, v, o));
+  if (lane == 0) m->red[wid][0] = v;
+  __syncthreads();
+  v = m->red[0][0];
+  for (int w = 1; w < NT / 32; ++w) v = min(v, m->red[w][0]);
+  __syncthreads();
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// occupied list (simulation.cu:41-64): 32 column stripes, stripe k = columns
+// k, k+32, ... < W-1 over rows 0..H-2, stripes concatenated in order.
+// Called by all threads; warp 0 builds.
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ void rebuild_list(uint8_t *st, uint16_t *list, Misc *m, int H, int W, int HW) {
+  for (int q = threadIdx.x; q < HW; q += NT) st[q] &= kStMask;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int k = threadIdx.x;
+    uint32_t cnt = 0;
+    for (int r = 0; r < H - 1; ++r)
+      for (int c = k; c < W - 1; c += 32) cnt += (st[r * W + c] & kStMask) == kOccupied;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(kFull, incl, o);
+      if (k >= o) incl += y;
+    }
+    uint32_t off = incl - cnt;
+    for (int r = 0; r < H - 1; ++r)
+      for (int c = k; c < W - 1; c += 32) {
+        int q = r * W + c;
+        if ((st[q] & kStMask) == kOccupied) {
+          list[off++] = (uint16_t)q;
+          st[q] |= kStRebuilt;
+        }
+      }
+    if (k == 31) {
+      m->n = incl;
+      m->n0 = incl;
+      m->has_multi = 0;
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// ROI + mask (diffusion.cu:16-100).  colmask[j] bit i = site (i, j) of the
+// (h+2) x (w+2) region is free (not held at the external level).
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ void compute_roi(const uint8_t *st, uint64_t *colmask, Misc *m, int H, int W, int HW) {
+  int v[4] = {H, W, 0, 0};
+  for (int q = threadIdx.x; q < HW; q += NT)
+    if ((st[q] & kStMask) == kOccupied) {
+      int r = q / W, c = q - (q / W) * W;
+      v[0] = min(v[0], r); v[1] = min(v[1], c);
+      v[2] = max(v[2], r); v[3] = max(v[3], c);
+    }
+  block_minmax4<NT>(v, m);
+  if (v[2] == 0 && v[3] == 0) {
+    if (threadIdx.x == 0) m->roi[0] = m->roi[1] = m->roi[2] = m->roi[3] = m->roi[4] = 0;
+    if (threadIdx.x < 64) colmask[threadIdx.x] = 0;
+    __syncthreads();
+    return;
+  }
+  const int midr = v[0] + (v[2] - v[0] + 1) / 2;
+  const int midc = v[1] + (v[3] - v[1] + 1) / 2;
+  int dist = 0;
+  for (int q = threadIdx.x; q < HW; q += NT)
+    if ((st[q] & kStMask) == kOccupied) {
+      int r = q / W, c = q - (q / W) * W;
+      float d2 = (float)((midr - r) * (midr - r) + (midc - c) * (midc - c));
+      dist = max(dist, (int)ceilf(sqrtf(d2)));
+    }
+  dist = block_max<NT>(dist, m);
+  const int sub_r = (midr <= dist) ? 1 : midr - dist;
+  const int sub_c = (midc <= dist) ? 1 : midc - dist;
+  const int sub_w = (midc + dist >= W - 1) ? W - 1 - sub_c : midc + dist - sub_c + 1;
+  const int sub_h = (midr + dist >= H - 1) ? H - 1 - sub_r : midr + dist - sub_r + 1;
+  if (threadIdx.x == 0) {
+    m->roi[0] = sub_r; m->roi[1] = sub_c; m->roi[2] = sub_h; m->roi[3] = sub_w; m->roi[4] = dist;
+  }
+  const int mh = sub_h + 2, mw = sub_w + 2;
+  const float mr = mh / 2.f, mc = mw / 2.f;
+  if (threadIdx.x < 64) {
+    const int j = threadIdx.x;
+    uint64_t bits = 0;
+    if (j < mw) {
+      const float fc = (float)(j + 1);
+      for (int i = 0; i < mh && i < 64; ++i) {
+        const float fr = (float)(i + 1);
+        const float d = sqrtf((fr - mr) * (fr - mr) + (fc - mc) * (fc - mc));
+        if (!(d >= (float)dist)) bits |= 1ull << i;
+      }
+    }
+    colmask[j] = bits;
+  }
+  __syncthreads();
+}
+
+// recompute the mask from a stored ROI (launch start between ROI updates)
+__device__ void restore_colmask(uint64_t *colmask, const Misc *m) {
+  if (threadIdx.x < 64) {
+    const int j = threadIdx.x, h = m->roi[2], w = m->roi[3], dist = m->roi[4];
+    uint64_t bits = 0;
+    if (h > 0 && w > 0) {
+      const int mh = h + 2, mw = w + 2;
+      const float mr = mh / 2.f, mc = mw / 2.f;
+      if (j < mw) {
+        const float fc = (float)(j + 1);
+        for (int i = 0; i < mh && i < 64; ++i) {
+          const float fr = (float)(i + 1);
+          const float d = sqrtf((fr - mr) * (fr - mr) + (fc - mc) * (fc - mc));
+          if (!(d >= (float)dist)) bits |= 1ull << i;
+        }
+      }
+    }
+    colmask[j] = bits;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// diffusion of one field by one warp of NP (part k = region rows
+// [k*RH, (k+1)*RH) of the (h+2) x (w+2) region; lane = column, or columns
+// 2*lane, 2*lane+1 when WIDE).
+// x' = a*x + b*(H + (x_up + x_down)) + d*(H_up + H_down), H = x_left + x_right.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void named_barrier(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+template <int NP, int RH, bool WIDE>
+__device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t *__restrict__ colmask,
+                                          float4 *__restrict__ xch, int part, int r0, int c0,
+                                          int h, int w, int nrow, int ncol, int W, float ext,
+                                          float ca, float cb, float cd, int nfree, int bar_id) {
+  const int lane = threadIdx.x & 31;
+  const int base = part * RH;
+  const int j0 = WIDE ? 2 * lane : lane;
+  const int j1 = 2 * lane + 1;
+  const int left = (lane + 31) & 31, right = (lane + 1) & 31;
+  const uint32_t rowsel = (1u << RH) - 1u;
+  const uint32_t fm0 = (j0 < ncol) ? (uint32_t)(colmask[j0] >> base) & rowsel : 0u;
+  const uint32_t fm1 = (WIDE && j1 < ncol) ? (uint32_t)(colmask[j1] >> base) & rowsel : 0u;
+  const uint32_t roirows = (uint32_t)(((((1ull << h) - 1ull) << 1)) >> base) & rowsel;
+  const uint32_t rm0 = (j0 >= 1 && j0 <= w) ? roirows : 0u;
+  const uint32_t rm1 = (WIDE && j1 >= 1 && j1 <= w) ? roirows : 0u;
+  const int lat0 = (r0 - 1) * W + (c0 - 1);
+
+  float x0[RH], x1[WIDE ? RH : 1];
+#pragma unroll
+  for (int i = 0; i < RH; ++i) {
+    const int gi = base + i;
+    const bool inr = gi < nrow;
+    x0[i] = (inr && j0 < ncol) ? (((fm0 >> i) & 1u) ? f[lat0 + gi * W + j0] : ext) : 0.f;
+    if (WIDE) x1[i] = (inr && j1 < ncol) ? (((fm1 >> i) & 1u) ? f[lat0 + gi * W + j1] : ext) : 0.f;
+  }
+
+  // xch[(part * 2 + parity) * 64 + side * 32 + lane]; side 0 = first row, 1 = last row
+  for (int s = 0; s <= nfree; ++s) {
+    const bool fin = (s == nfree);
+    const uint32_t u0 = fin ? rm0 : fm0;
+    const uint32_t u1 = fin ? rm1 : fm1;
+    const int par = s & 1;
+    {
+      float ht0, ht1 = 0.f, hb0, hb1 = 0.f;
+      if (WIDE) {
+        ht0 = __shfl_sync(kFull, x1[0], left) + x1[0];
+        ht1 = x0[0] + __shfl_sync(kFull, x0[0], right);
+        hb0 = __shfl_sync(kFull, x1[RH - 1], left) + x1[RH - 1];
+        hb1 = x0[RH - 1] + __shfl_sync(kFull, x0[RH - 1], right);
+      } else {
+        ht0 = __shfl_sync(kFull, x0[0], left) + __shfl_sync(kFull, x0[0], right);
+        hb0 = __shfl_sync(kFull, x0[RH - 1], left) + __shfl_sync(kFull, x0[RH - 1], right);
+      }
+      float4 *mine = xch + (part * 2 + par) * 64 + lane;
+      if (part > 0) mine[0] = make_float4(x0[0], ht0, WIDE ? x1[0] : 0.f, ht1);
+      if (part < NP - 1) mine[32] = make_float4(x0[RH - 1], hb0, WIDE ? x1[RH - 1] : 0.f, hb1);
+    }
+    named_barrier(bar_id, NP * 32);
+    float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), nx = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (part > 0) pv = xch[((part - 1) * 2 + par) * 64 + 32 + lane];
+    if (part < NP - 1) nx = xch[((part + 1) * 2 + par) * 64 + lane];
+
+    float xm0 = pv.x, hm0 = pv.y, xm1 = pv.z, hm1 = pv.w;
+    float hc0, hc1 = 0.f;
+    if (WIDE) {
+      hc0 = __shfl_sync(kFull, x1[0], left) + x1[0];
+      hc1 = x0[0] + __shfl_sync(kFull, x0[0], right);
+    } else {
+      hc0 = __shfl_sync(kFull, x0[0], left) + __shfl_sync(kFull, x0[0], right);
+    }
+#pragma unroll
+    for (int i = 0; i < RH; ++i) {
+      float xn0, hn0, xn1 = 0.f, hn1 = 0.f;
+      if (i + 1 < RH) {
+        xn0 = x0[i + 1];
+        if (WIDE) {
+          xn1 = x1[i + 1];
+          hn0 = __shfl_sync(kFull, xn1, left) + xn1;
+          hn1 = xn0 + __shfl_sync(kFull, xn0, right);
+        } else {
+          hn0 = __shfl_sync(kFull, xn0, left) + __shfl_sync(kFull, xn0, right);
+        }
+      } else {
+        xn0 = nx.x; hn0 = nx.y; xn1 = nx.z; hn1 = nx.w;
+      }
+      const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0 + (xm0 + xn0), cd * (hm0 + hn0)));
+      xm0 = x0[i];
+      if ((u0 >> i) & 1u) x0[i] = nv0;
+      hm0 = hc0;
+      hc0 = hn0;
+      if (WIDE) {
+        const float nv1 = fmaf(ca, x1[i], fmaf(cb, hc1 + (xm1 + xn1), cd * (hm1 + hn1)));
+        xm1 = x1[i];
+        if ((u1 >> i) & 1u) x1[i] = nv1;
+        hm1 = hc1;
+        hc1 = hn1;
+      }
+    }
+  }
+  // write back the ROI interior
+#pragma unroll
+  for (int i = 0; i < RH; ++i) {
+    const int gi = base + i;
+    if (gi >= 1 && gi <= h) {
+      if (j0 >= 1 && j0 <= w) f[lat0 + gi * W + j0] = x0[i];
+      if (WIDE && j1 >= 1 && j1 <= w) f[lat0 + gi * W + j1] = x1[i];
+    }
+  }
+}
+
+// NP warps per field; warp w diffuses field w / NP, part w % NP.
+// The caller guarantees 2*NP*RH_max >= nrow and (WIDE_OK or ncol <= 31).
+template <int NP, bool WIDE_OK>
+__device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask, float4 *xch,
+                                             const Misc *m, const KParams &p) {
+  const int r0 = m->roi[0], c0 = m->roi[1], h = m->roi[2], w = m->roi[3];
+  if (h == 0 || w == 0) return;
+  const int nrow = h + 2, ncol = w + 2;
+  const int wid = threadIdx.x >> 5;
+  const int field = wid / NP, part = wid % NP;
+  int RH = (nrow + NP - 1) / NP;
+  RH = (RH + 1) & ~1;
+  float *f = fld + field * p.HW;
+  float4 *x = xch + field * NP * 128;
+  const float ext = p.ext[field], ca = p.da[field], cb = p.db[field], cd = p.dd[field];
+  const int nf = p.nfree, bar = 1 + field, W = p.W;
+#define EMT6_CALL(R, WD)                                                                   \
+  diffuse_part<NP, R, WD>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, \
+                          nf, bar)
+#define EMT6_CASES(WD)                   \
+  switch (RH) {                          \
+    case 2: EMT6_CALL(2, WD); break;     \
+    case 4: EMT6_CALL(4, WD); break;     \
+    case 6: EMT6_CALL(6, WD); break;     \
+    case 8: EMT6_CALL(8, WD); break;     \
+    case 10: EMT6_CALL(10, WD); break;   \
+    case 12: EMT6_CALL(12, WD); break;   \
+    case 14: EMT6_CALL(14, WD); break;   \
+    default:                             \
+      if constexpr (NP == 2) {           \
+        if (RH == 16) EMT6_CALL(16, WD); \
+      }                                  \
+      break;                             \
+  }
+  if (!WIDE_OK || ncol <= 31) {
+    EMT6_CASES(false)
+  } else {
+    EMT6_CASES(WIDE_OK)
+  }
+#undef EMT6_CASES
+#undef EMT6_CALL
+}
+
+// ---------------------------------------------------------------------------
+// Site::step (site/site.h:62-82) on the CTA's lattice; returns ready-to-divide.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool step_site(const KParams &p, float *fld, uint8_t *st,
+                                          float4 *cells, int s, uint32_t vac, float dose,
+                                          uint32_t t, uint32_t sim, uint32_t occ,
+                                          uint32_t epoch, Misc *m) {
+  DCell c = load_cell(cells + 3 * s);
+  const int HW = p.HW;
+  float l0 = fld[s], l1 = fld[HW + s], l2 = fld[2 * HW + s];
+  if (!update_state(c, l0, l1, l2, p, vac)) {
+    st[s] = (st[s] & ~kStMask) | kVacant;
+    return false;
+  }
+  if (dose > 0) {
+    irradiate(c, dose, p);
+    atomicAdd(&m->ins[2], 1u);
+  }
+  l0 -= p.met[c.mode][0];
+  l1 -= p.met[c.mode][1];
+  l2 -= p.met[c.mode][2];
+  fld[s] = l0;
+  fld[HW + s] = l1;
+  fld[2 * HW + s] = l2;
+  const bool cc = progress_clock(c, p);
+  bool dead = false;
+  if (repair_pre(c, p, cc)) {
+    const float dp = death_prob(c, p);
+    atomicAdd(&m->ins[0], 1u);
+    atomicAdd(&m->ins_dp, (double)dp);
+    int bi = (int)(c.irr / 0.1f);
+    bi = bi < 0 ? 0 : (bi >= 300 ? 299 : bi);
+    int bj = (int)(c.tir / 0.1f);
+    bj = bj < 0 ? 0 : (bj >= 300 ? 299 : bj);
+    atomicAdd(&g_instr_hist[bi], 1ull);
+    atomicAdd(&g_instr_hist[300 + bj], 1ull);
+    const float u = u01(draw(p, t, sim, (uint32_t)s, occ, 1, epoch).x);
+    if (u < dp) {
+      dead = true;
+      atomicAdd(&m->ins[1], 1u);
+    } else {
+      c.irr = 0.f;
+      c.tir = 0.f;
+      c.delay = 0.f;
+    }
+  }
+  store_cell(cells + 3 * s, c);
+  if (dead) {
+    st[s] = (st[s] & ~kStMask) | kVacant;
+    return false;
+  }
+  return c.phase == 4;
+}
+
+// occurrence index of list entry e of a multi-listed site (entries before e
+// with the same site): 0 in the rebuilt part, else rebuilt-bit + tail count.
+__device__ __forceinline__ uint32_t occurrence(const uint16_t *list, const uint8_t *st, uint32_t e,
+                                               uint32_t n0) {
+  const int lane = threadIdx.x & 31;
+  const uint16_t s = list[e];
+  if (e < n0) return 0;
+  uint32_t k = (st[s] & kStRebuilt) ? 1u : 0u;
+  for (uint32_t b = n0; b < e; b += 32) {
+    const uint32_t q = b + lane;
+    k += __popc(__ballot_sync(kFull, q < e && list[q] == s));
+  }
+  return k;
+}
+
+// ---------------------------------------------------------------------------
+// the fused step kernel
+// ---------------------------------------------------------------------------
+// WIDE_OK = false: 192 threads, two warps per field, regions up to 32 x 31
+// (4 CTAs/SM); a simulation whose region grows beyond that is parked at the
+// start of that step for the WIDE_OK = true kernel: 384 threads, four warps
+// per field, regions up to 56 x 62 (2 CTAs/SM).
+template <bool WIDE_OK>
+__global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
+    run_kernel(const RunArgs a, uint32_t t_end) {
+  constexpr int NT = WIDE_OK ? 384 : 192;
+  constexpr int NP = NT / 96;
+  extern __shared__ __align__(16) uint8_t sm[];
+  const KParams &p = a.p;
+  const int H = p.H, W = p.W, HW = p.HW;
+  const SmemLayout L = smem_layout(HW, p.lcap, NP);
+  float *fld = reinterpret_cast<float *>(sm + L.fld);
+  uint8_t *st = sm + L.st;
+  uint16_t *list = reinterpret_cast<uint16_t *>(sm + L.list);
+  uint8_t *aux = sm + L.aux;
+  uint64_t *colmask = reinterpret_cast<uint64_t *>(sm + L.colmask);
+  float4 *xch = reinterpret_cast<float4 *>(sm + L.xch);
+  Misc *m = reinterpret_cast<Misc *>(sm + L.misc);
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+
+  for (int64_t item = blockIdx.x;; item += gridDim.x) {
+    int64_t sim;
+    if (a.queue) {
+      // persistent CTAs: take the next simulation from the work queue
+      __syncthreads();
+      if (tid == 0) m->winner = (int)atomicAdd(a.ticket, 1u);
+      __syncthreads();
+      const int64_t ticket = m->winner;
+      if (ticket >= a.nsims) break;
+      sim = a.order[ticket];
+    } else {
+      if (item >= a.nsims) break;
+      sim = item;
+    }
+    {
+      // nothing to do for a simulation already at its target step
+      const uint32_t hz = a.horizon ? a.horizon[sim] : 0xFFFFFFFFu;
+      if (a.step[sim] >= (t_end < hz ? t_end : hz)) continue;
+    }
+
+    // ---- load the simulation into shared memory ----
+    const float4 *gf = reinterpret_cast<const float4 *>(a.fld + sim * a.fstride);
+    for (uint32_t q = tid; q < a.fstride / 4; q += NT)
+      reinterpret_cast<float4 *>(fld)[q] = gf[q];
+    const uint4 *gs = reinterpret_cast<const uint4 *>(a.st + sim * a.sstride);
+    for (uint32_t q = tid; q < a.sstride / 16; q += NT)
+      reinterpret_cast<uint4 *>(st)[q] = gs[q];
+    const int4 meta = a.meta[sim];
+    const uint16_t *gl = a.list + sim * a.lstride;
+    for (int q = tid; q < meta.x; q += NT) list[q] = gl[q];
+    if (tid == 0) {
+      m->n = (uint32_t)meta.x;
+      m->n0 = (uint32_t)meta.y;
+      m->has_multi = meta.z;
+      for (int k = 0; k < 5; ++k) m->roi[k] = a.roi[sim * 8 + k];
+      m->ins[0] = m->ins[1] = m->ins[2] = m->ins[3] = 0;
+      m->ins_dp = 0.0;
+      m->diffused = 0;
+    }
+    __syncthreads();
+    restore_colmask(colmask, m);
+    __syncthreads();
+    if (tid == 0) {
+      unsigned long long nf = 0;
+      for (int j = 0; j < 64; ++j) nf += __popcll(colmask[j]);
+      m->nfs = nf;
+    }
+    float4 *cells = a.cell + sim * (int64_t)HW * 3;
+    const uint32_t step0 = a.step[sim];
+    const uint32_t horizon = a.horizon ? a.horizon[sim] : 0xFFFFFFFFu;
+    const int32_t prot = a.sim_protocol[sim];
+    const float *doses = a.doses + (int64_t)prot * p.bins;
+    uint32_t t = step0;
+    __syncthreads();
+
+    const uint32_t t_stop = t_end < horizon ? t_end : horizon;
+    for (; t < t_stop; ++t) {
+      if (t % 128 == 0) rebuild_list<NT>(st, list, m, H, W, HW);
+      if (t % 32 == 0) {
+        compute_roi<NT>(st, colmask, m, H, W, HW);
+        if (tid == 0) {
+          unsigned long long nf = 0;
+          for (int j = 0; j < 64; ++j) nf += __popcll(colmask[j]);
+          m->nfs = nf;
+        }
+      }
+      // a region wider than 31 columns is left for the wide-capable kernel;
+      // the state stored is the state at the start of step t (the list
+      // rebuild and ROI above are recomputed identically there)
+      if (!WIDE_OK && (m->roi[3] + 2 > 31 || m->roi[2] + 2 > 32)) break;
+      // vacancy snapshot (simulation.cu:79-83), before any site changes
+      const uint32_t n = m->n;
+      for (uint32_t e = tid; e < n; e += NT) {
+        const int s = list[e];
+        aux[e] = (uint8_t)(((st[s - W - 1] & kStMask) == kVacant) +
+                           ((st[s - W + 1] & kStMask) == kVacant) +
+                           ((st[s + W - 1] & kStMask) == kVacant) +
+                           ((st[s + W + 1] & kStMask) == kVacant) +
+                           ((st[s - 1] & kStMask) == kVacant) + ((st[s + 1] & kStMask) == kVacant) +
+                           ((st[s - W] & kStMask) == kVacant) + ((st[s + W] & kStMask) == kVacant));
+      }
+      diffuse_step<NP, WIDE_OK>(fld, colmask, xch, m, p);
+      // diffused site-substeps: free sites x free substeps + the final ROI pass
+      if (tid == 0 && m->roi[2] > 0)
+        m->diffused += m->nfs * (unsigned long long)p.nfree +
+                       (unsigned long long)m->roi[2] * (unsigned long long)m->roi[3];
+      __syncthreads();
+
+      // ---- cell update (simulation.cu:84-96) ----
+      const float dose =
+          (t < p.length && t % p.res == 0 && t / p.res < p.bins) ? doses[t / p.res] : 0.f;
+      for (uint32_t e = tid; e < n; e += NT) {
+        const int s = list[e];
+        const uint8_t sv = st[s];
+        if ((sv & kStMask) != kOccupied) {
+          if (!(sv & kStMulti)) aux[e] = 0;
+          continue;
+        }
+        if (sv & kStMulti) continue;  // stepped in list order below
+        const bool ready = step_site(p, fld, st, cells, s, aux[e], dose, t, (uint32_t)sim, 0,
+                                     a.epoch, m);
+        aux[e] = ready ? 0x80 : 0;
+      }
+      if (m->has_multi && wid == 0) {
+        // sites listed more than once: every entry steps the site, in list order
+        const uint32_t n0 = m->n0;
+        for (uint32_t b = 0; b < n; b += 32) {
+          const uint32_t e = b + lane;
+          const bool mult = e < n && (st[list[e]] & kStMulti);
+          uint32_t bal = __ballot_sync(kFull, mult);
+          while (bal) {
+            const int bit = __ffs(bal) - 1;
+            bal &= bal - 1;
+            const uint32_t ee = b + bit;
+            const uint32_t occ = occurrence(list, st, ee, n0);
+            if (lane == 0) {
+              const int s = list[ee];
+              uint8_t res = 0;
+              if ((st[s] & kStMask) == kOccupied) {
+                const bool ready = step_site(p, fld, st, cells, s, aux[ee] & 15u, dose, t,
+                                             (uint32_t)sim, occ, a.epoch, m);
+                if (ready) {
+                  if (occ > 127) atomicOr(a.err, 4u);
+                  res = (uint8_t)(0x80 | (occ & 0x7f));
+                }
+              }
+              aux[ee] = res;
+            }
+            __syncwarp();
+          }
+        }
+      }
+      __syncthreads();
+
+      // ---- division arbitration: lowest list index with a vacant target ----
+      int best = 0x7fffffff, best_target = -1;
+      for (uint32_t e = tid; e < n; e += NT) {
+        const uint8_t av = aux[e];
+        if (av & 0x80) {
+          const int s = list[e];
+          const float u = u01(draw(p, t, (uint32_t)sim, (uint32_t)s, av & 0x7fu, 0, a.epoch).x);
+          const int tg = choose_neighbour(s, W, u);
+          if ((st[tg] & kStMask) == kVacant) {
+            best = (int)e;
+            best_target = tg;
+            break;
+          }
+        }
+      }
+      const int win = block_min<NT>(best, m);
+      if (win != 0x7fffffff && best == win) {
+        m->winner = win;
+        m->target = best_target;
+      }
+      __syncthreads();
+      if (win != 0x7fffffff && wid == 0) {
+        // divideCell (cell-division.h:10-30) with five Philox normals; lanes
+        // 0..2 each evaluate one Box-Muller pair
+        float za = 0.f, zb = 0.f;
+        if (lane < 3) {
+          const uint4 r = draw(p, t, (uint32_t)sim, 0xFFFFu, 0, lane == 2 ? 3 : 2, a.epoch);
+          if (lane == 0) box_muller(r.x, r.y, &za, &zb);
+          else if (lane == 1) box_muller(r.z, r.w, &za, &zb);
+          else box_muller(r.x, r.y, &za, &zb);
+        }
+        float z[5];
+        z[0] = __shfl_sync(kFull, za, 0);
+        z[1] = __shfl_sync(kFull, zb, 0);
+        z[2] = __shfl_sync(kFull, za, 1);
+        z[3] = __shfl_sync(kFull, zb, 1);
+        z[4] = __shfl_sync(kFull, za, 2);
+        if (lane == 0) {
+          const int parent = list[m->winner], child = m->target;
+          DCell pc = load_cell(cells + 3 * parent);
+          pc.phase = 0;
+          pc.prolif = 0.f;
+          store_cell(cells + 3 * parent, pc);
+          const DCell cc = make_child(pc, z, p);
+          store_cell(cells + 3 * child, cc);
+          const uint8_t sv = st[child];
+          const bool listed = (sv & (kStRebuilt | kStTail)) != 0;
+          st[child] = (uint8_t)((sv & (kStRebuilt | kStTail | kStMulti)) | kStTail |
+                                (listed ? kStMulti : 0) | kOccupied);
+          if (listed) m->has_multi = 1;
+          if (m->n < (uint32_t)p.lcap) list[m->n++] = (uint16_t)child;
+          else atomicOr(a.err, 1u);
+          m->ins[3] += 1;
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- write the simulation back ----
+    float4 *of = reinterpret_cast<float4 *>(a.fld + sim * a.fstride);
+    for (uint32_t q = tid; q < a.fstride / 4; q += NT)
+      of[q] = reinterpret_cast<const float4 *>(fld)[q];
+    uint4 *os = reinterpret_cast<uint4 *>(a.st + sim * a.sstride);
+    for (uint32_t q = tid; q < a.sstride / 16; q += NT)
+      os[q] = reinterpret_cast<const uint4 *>(st)[q];
+    uint16_t *ol = a.list + sim * a.lstride;
+    for (uint32_t q = tid; q < m->n; q += NT) ol[q] = list[q];
+    int live = 0;
+    for (int q = tid; q < HW; q += NT) live += (st[q] & kStMask) == kOccupied;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) live += __shfl_xor_sync(kFull, live, o);
+    __syncthreads();
+    if (lane == 0) m->red[wid][1] = live;
+    __syncthreads();
+    if (tid == 0) {
+      int tot = 0;
+      for (int w2 = 0; w2 < NT / 32; ++w2) tot += m->red[w2][1];
+      a.counts[sim] = (uint32_t)tot;
+      a.meta[sim] = make_int4((int)m->n, (int)m->n0, m->has_multi, 0);
+      for (int k2 = 0; k2 < 5; ++k2) a.roi[sim * 8 + k2] = m->roi[k2];
+      a.step[sim] = t;
+      if (m->ins[0]) atomicAdd(&g_instr_counts[0], (unsigned long long)m->ins[0]);
+      if (m->ins[1]) atomicAdd(&g_instr_counts[1], (unsigned long long)m->ins[1]);
+      if (m->ins[2]) atomicAdd(&g_instr_counts[2], (unsigned long long)m->ins[2]);
+      if (m->ins[3]) atomicAdd(&g_instr_counts[3], (unsigned long long)m->ins[3]);
+      if (m->ins_dp != 0.0) atomicAdd(&g_instr_sum_death_prob, m->ins_dp);
+      if (m->diffused) atomicAdd(a.diffused, m->diffused);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// reset: expand the initial tumours into every simulation
+// ---------------------------------------------------------------------------
+__global__ void reset_kernel(const ResetArgs a) {
+  for (int64_t sim = blockIdx.x; sim < a.nsims; sim += gridDim.x) {
+    const int t = a.sim_tumor[sim];
+    const float4 *sf = reinterpret_cast<const float4 *>(a.tpl_fld + (int64_t)t * a.fstride);
+    float4 *df = reinterpret_cast<float4 *>(a.fld + sim * a.fstride);
+    for (uint32_t q = threadIdx.x; q < a.fstride / 4; q += blockDim.x) df[q] = sf[q];
+    const uint4 *ss = reinterpret_cast<const uint4 *>(a.tpl_st + (int64_t)t * a.sstride);
+    uint4 *ds = reinterpret_cast<uint4 *>(a.st + sim * a.sstride);
+    for (uint32_t q = threadIdx.x; q < a.sstride / 16; q += blockDim.x) ds[q] = ss[q];
+    const float4 *sc = a.tpl_cell + (int64_t)t * a.HW * 3;
+    float4 *dc = a.cell + sim * (int64_t)a.HW * 3;
+    for (int q = threadIdx.x; q < a.HW * 3; q += blockDim.x) dc[q] = sc[q];
+    if (threadIdx.x == 0) {
+      a.meta[sim] = make_int4(0, 0, 0, 0);
+      for (int k = 0; k < 8; ++k) a.roi[sim * 8 + k] = 0;
+      a.step[sim] = 0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// unit hooks: run the device functions above on caller-provided inputs
+// ---------------------------------------------------------------------------
+__global__ void test_philox_kernel(const uint4 *ctr, const uint2 *key, uint4 *out, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = philox4x32_10(ctr[i], key[i].x, key[i].y);
+}
+
+__global__ void test_math_kernel(const float *x, float *ex, const double *u, double *lg, double *sn,
+                                 double *cs, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) {
+    ex[i] = dexpf(x[i]);
+    lg[i] = log_core(u[i] > 0 ? u[i] : 1.0);
+    double s, c;
+    double v = u[i] - floor(u[i]);
+    sincos2pi(v, &s, &c);
+    sn[i] = s;
+    cs[i] = c;
+  }
+}
+
+__global__ void test_site_step_kernel(const KParams p, float4 *cells, float *lv, uint8_t *state,
+                                      const uint32_t *vac, const float *dose, const float *draws,
+                                      int32_t *ready, int32_t *used, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  ready[i] = 0;
+  used[i] = 0;
+  if (state[i] != kOccupied) return;
+  DCell c = load_cell(cells + 3 * i);
+  float l0 = lv[3 * i], l1 = lv[3 * i + 1], l2 = lv[3 * i + 2];
+  if (!update_state(c, l0, l1, l2, p, vac[i])) {
+    state[i] = kVacant;
+    store_cell(cells + 3 * i, c);
+    return;
+  }
+  if (dose[i] > 0) irradiate(c, dose[i], p);
+  l0 -= p.met[c.mode][0];
+  l1 -= p.met[c.mode][1];
+  l2 -= p.met[c.mode][2];
+  lv[3 * i] = l0; lv[3 * i + 1] = l1; lv[3 * i + 2] = l2;
+  const bool cc = progress_clock(c, p);
+  bool dead = false;
+  if (repair_pre(c, p, cc)) {
+    used[i] = 1;
+    if (draws[i] < death_prob(c, p)) dead = true;
+    else { c.irr = 0.f; c.tir = 0.f; c.delay = 0.f; }
+  }
+  store_cell(cells + 3 * i, c);
+  if (dead) state[i] = kVacant;
+  else ready[i] = c.phase == 4;
+}
+
+__global__ void test_choose_kernel(const float *u, int r, int c, int W, int32_t *rc, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) {
+    int s = choose_neighbour(r * W + c, W, u[i]);
+    rc[2 * i] = s / W;
+    rc[2 * i + 1] = s % W;
+  }
+}
+
+__global__ void test_divide_kernel(const KParams p, float4 *parents, const float *z,
+                                   float4 *children, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  DCell pc = load_cell(parents + 3 * i);
+  pc.phase = 0;
+  pc.prolif = 0.f;
+  store_cell(parents + 3 * i, pc);
+  float zz[5] = {z[5 * i], z[5 * i + 1], z[5 * i + 2], z[5 * i + 3], z[5 * i + 4]};
+  store_cell(children + 3 * i, make_child(pc, zz, p));
+}
+
+__global__ void test_normals_kernel(const KParams p, const uint32_t *step, const uint32_t *sim,
+                                    uint32_t epoch, float *z, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint4 r1 = draw(p, step[i], sim[i], 0xFFFFu, 0, 2, epoch);
+  const uint4 r2 = draw(p, step[i], sim[i], 0xFFFFu, 0, 3, epoch);
+  float unused;
+  box_muller(r1.x, r1.y, &z[5 * i], &z[5 * i + 1]);
+  box_muller(r1.z, r1.w, &z[5 * i + 2], &z[5 * i + 3]);
+  box_muller(r2.x, r2.y, &z[5 * i + 4], &unused);
+}
+
+// one CTA: list rebuild + ROI on a lattice, or one diffusion step with the
+// narrow (WIDE_OK = false) or wide kernel's diffusion path
+template <bool WIDE_OK>
+__global__ void __launch_bounds__(WIDE_OK ? 384 : 192)
+    test_block_kernel(const KParams p, int mode, float *gfld, const uint8_t *gst, int32_t *roi,
+                      uint8_t *mask, uint16_t *glist, uint32_t *gn) {
+  constexpr int NT = WIDE_OK ? 384 : 192;
+  constexpr int NP = NT / 96;
+  extern __shared__ __align__(16) uint8_t sm[];
+  const int HW = p.HW;
+  const SmemLayout L = smem_layout(HW, p.lcap, NP);
+  float *fld = reinterpret_cast<float *>(sm + L.fld);
+  uint8_t *st = sm + L.st;
+  uint16_t *list = reinterpret_cast<uint16_t *>(sm + L.list);
+  uint64_t *colmask = reinterpret_cast<uint64_t *>(sm + L.colmask);
+  float4 *xch = reinterpret_cast<float4 *>(sm + L.xch);
+  Misc *m = reinterpret_cast<Misc *>(sm + L.misc);
+  for (int q = threadIdx.x; q < HW; q += NT) st[q] = gst ? gst[q] : 0;
+  if (gfld)
+    for (int q = threadIdx.x; q < 3 * HW; q += NT) fld[q] = gfld[q];
+  __syncthreads();
+  if (mode == 0) {
+    rebuild_list<NT>(st, list, m, p.H, p.W, HW);
+    for (uint32_t q = threadIdx.x; q < m->n; q += NT) glist[q] = list[q];
+    if (threadIdx.x == 0) *gn = m->n;
+  } else if (mode == 1) {
+    compute_roi<NT>(st, colmask, m, p.H, p.W, HW);
+    if (threadIdx.x == 0)
+      for (int k = 0; k < 5; ++k) roi[k] = m->roi[k];
+    const int mh = m->roi[2] + 2, mw = m->roi[3] + 2;
+    if (m->roi[2] > 0)
+      for (int q = threadIdx.x; q < mh * mw; q += NT) {
+        int i = q / mw, j = q % mw;
+        mask[q] = ((colmask[j] >> i) & 1ull) ? 0 : 1;
+      }
+  } else {
+    if (threadIdx.x == 0)
+      for (int k = 0; k < 5; ++k) m->roi[k] = roi[k];
+    __syncthreads();
+    restore_colmask(colmask, m);
+    __syncthreads();
+    diffuse_step<NP, WIDE_OK>(fld, colmask, xch, m, p);
+    __syncthreads();
+    for (int q = threadIdx.x; q < 3 * HW; q += NT) gfld[q] = fld[q];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+// ---------------------------------------------------------------------------
+cudaError_t launch_run(const RunArgs &a, uint32_t t_end, bool wide, int grid,
+                       cudaStream_t stream) {
+  const size_t smem = run_kernel_smem(a.p.HW, a.p.lcap, wide);
+  cudaError_t e;
+  if (wide) {
+    e = cudaFuncSetAttribute(run_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return e;
+    run_kernel<true><<<grid, 384, smem, stream>>>(a, t_end);
+  } else {
+    e = cudaFuncSetAttribute(run_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return e;
+    run_kernel<false><<<grid, 192, smem, stream>>>(a, t_end);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reset(const ResetArgs &a, cudaStream_t stream) {
+  int grid = (int)(a.nsims < 65535 * 8 ? a.nsims : 65535 * 8);
+  if (grid < 1) return cudaSuccess;
+  reset_kernel<<<grid, 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+int max_ctas_per_sm(const KParams &p, bool wide) {
+  const size_t smem = run_kernel_smem(p.HW, p.lcap, wide);
+  int n = 0;
+  if (wide) {
+    cudaFuncSetAttribute(run_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, run_kernel<true>, 384, smem) !=
+        cudaSuccess)
+      return 0;
+  } else {
+    cudaFuncSetAttribute(run_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, run_kernel<false>, 192, smem) !=
+        cudaSuccess)
+      return 0;
+  }
+  return n;
+}
+
+cudaError_t instr_read(unsigned long long counts[4], double *sum_dp, unsigned long long *hist) {
+  cudaError_t e = cudaMemcpyFromSymbol(counts, g_instr_counts, sizeof(unsigned long long) * 4);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyFromSymbol(sum_dp, g_instr_sum_death_prob, sizeof(double));
+  if (e != cudaSuccess) return e;
+  if (hist) e = cudaMemcpyFromSymbol(hist, g_instr_hist, sizeof(unsigned long long) * 600);
+  return e;
+}
+
+cudaError_t instr_reset() {
+  unsigned long long z[600] = {0};
+  double zd = 0.0;
+  cudaError_t e = cudaMemcpyToSymbol(g_instr_counts, z, sizeof(unsigned long long) * 4);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyToSymbol(g_instr_sum_death_prob, &zd, sizeof(double));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(g_instr_hist, z, sizeof(z));
+}
+
+cudaError_t launch_test_philox(const uint4 *c, const uint2 *k, uint4 *o, int64_t n) {
+  test_philox_kernel<<<(unsigned)((n + 127) / 128), 128>>>(c, k, o, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_test_math(const float *x, float *ex, const double *u, double *lg, double *sn,
+                             double *cs, int64_t n) {
+  test_math_kernel<<<(unsigned)((n + 127) / 128), 128>>>(x, ex, u, lg, sn, cs, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_test_site_step(const KParams &p, float4 *cells, float *lv, uint8_t *state,
+                                  const uint32_t *vac, const float *dose, const float *draws,
+                                  int32_t *ready, int32_t *used, int64_t n) {
+  test_site_step_kernel<<<(unsigned)((n + 127) / 128), 128>>>(p, cells, lv, state, vac, dose,
+                                                               draws, ready, used, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_test_choose(const float *u, int r, int c, int W, int32_t *rc, int64_t n) {
+  test_choose_kernel<<<(unsigned)((n + 127) / 128), 128>>>(u, r, c, W, rc, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_test_divide(const KParams &p, float4 *parents, const float *z, float4 *children,
+                               int64_t n) {
+  test_divide_kernel<<<(unsigned)((n + 127) / 128), 128>>>(p, parents, z, children, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_test_normals(const KParams &p, const uint32_t *step, const uint32_t *sim,
+                                uint32_t epoch, float *z, int64_t n) {
+  test_normals_kernel<<<(unsigned)((n + 127) / 128), 128>>>(p, step, sim, epoch, z, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_test_block(const KParams &p, int mode, bool wide, float *fld,
+                              const uint8_t *st, int32_t *roi, uint8_t *mask, uint16_t *list,
+                              uint32_t *n) {
+  const size_t smem = run_kernel_smem(p.HW, p.lcap, wide);
+  cudaError_t e;
+  if (wide) {
+    e = cudaFuncSetAttribute(test_block_kernel<true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    test_block_kernel<true><<<1, 384, smem>>>(p, mode, fld, st, roi, mask, list, n);
+  } else {
+    e = cudaFuncSetAttribute(test_block_kernel<false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    test_block_kernel<false><<<1, 192, smem>>>(p, mode, fld, st, roi, mask, list, n);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace emt6

@@ -1,0 +1,121 @@
+"""Whole-simulation parity: the fused CUDA step kernels vs the CPU oracle,
+bit-exact on every lattice field and on the living counts, across the list
+rebuild (128 steps) and ROI (32 steps) cadences, irradiation, chunked runs,
+resets, regions that need the wide kernel, ragged horizons and the
+work-queue schedule."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_pair(params, oracle, tumors, protocols, sim_tumor, sim_protocol, steps, seed,
+              horizon=None, chunks=None, schedule=0, epoch=0):
+    from emt6ro.batch import Batch
+    b = Batch(params, tumors, protocols, sim_tumor, sim_protocol, sim_horizon=horizon, seed=seed)
+    if schedule:
+        b.set_schedule(schedule, 0)
+    for c in (chunks or [steps]):
+        b.run(c)
+    counts = b.counts()
+    n = len(sim_tumor)
+    ob = oracle.Batch(oracle.params_copy(params.native), n, seed)
+    for i in range(n):
+        hz = 0xFFFFFFFF if horizon is None else int(horizon[i])
+        ob.set(i, tumors[sim_tumor[i]].sites, b.doses[sim_protocol[i]], resolution=300,
+               length=144_000, epoch=epoch, horizon=hz)
+    ob.run(steps, nthreads=8)
+    return b, ob, counts, ob.counts()
+
+
+def _assert_same(b, ob, n):
+    for i in range(n):
+        g = b.state(i).sites
+        o = ob.get(i)
+        if g.tobytes() != o.tobytes():
+            bad = [f for f in g.dtype.names if np.ascontiguousarray(g[f]).tobytes()
+                   != np.ascontiguousarray(o[f]).tobytes()]
+            raise AssertionError(f"simulation {i}: fields {bad} differ from the oracle")
+
+
+def test_small_batch_bit_exact(params, oracle):
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, r, seed=s) for r, s in ((5, 1), (9, 2), (12, 3))]
+    protocols = [[], [(600, 1.25), (1500, 2.5)], [(0, 5.0)]]
+    st = np.array([0, 1, 2, 0, 1, 2, 2, 1], np.int32)
+    sp = np.array([0, 1, 2, 1, 2, 0, 1, 2], np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 2000, seed=77)
+    assert (c == co).all(), (c, co)
+    _assert_same(b, ob, len(st))
+
+
+def test_chunked_runs_equal_one_run(params, oracle):
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, 10, seed=9)]
+    protocols = [[(300, 2.0), (1200, 2.0)]]
+    st = np.zeros(4, np.int32)
+    sp = np.zeros(4, np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 1500, seed=5,
+                             chunks=[1, 31, 96, 100, 500, 772])
+    assert (c == co).all()
+    _assert_same(b, ob, 4)
+
+
+def test_wide_regions_bit_exact(params, oracle):
+    """Tumours whose region exceeds 32 x 31 run on the 384-thread kernel."""
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, 17, seed=11), wl.disc_tumor(params, 22, seed=12),
+              wl.disc_tumor(params, 14, seed=13, center=(20, 30))]
+    protocols = [[(0, 2.0), (600, 2.0)]]
+    st = np.array([0, 1, 2, 1], np.int32)
+    sp = np.zeros(4, np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 700, seed=21)
+    assert (c == co).all()
+    _assert_same(b, ob, 4)
+
+
+def test_ragged_horizons_and_queue(params, oracle):
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, r, seed=30 + r) for r in (2, 7, 18)]
+    protocols = [[], [(100, 3.0)], [(50, 1.0), (400, 1.0), (800, 1.0)]]
+    st = np.array([0, 1, 2, 1, 2, 0], np.int32)
+    sp = np.array([1, 2, 0, 0, 1, 2], np.int32)
+    hz = np.array([100, 900, 450, 1000, 33, 700], np.uint32)
+    for sched in (0, 1):
+        b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 1000, seed=3,
+                                 horizon=hz, schedule=sched)
+        assert (c == co).all()
+        _assert_same(b, ob, len(st))
+        for i in range(len(st)):
+            assert b.step(i) == min(1000, int(hz[i]))
+
+
+def test_reset_gives_fresh_epoch(params, oracle):
+    from emt6ro import workloads as wl
+    from emt6ro.batch import Batch
+    tumors = [wl.disc_tumor(params, 9, seed=2)]
+    protocols = [[(60, 2.5)]]
+    st = np.zeros(3, np.int32)
+    sp = np.zeros(3, np.int32)
+    b = Batch(params, tumors, protocols, st, sp, seed=99)
+    b.run(400)
+    first = [b.state(i).sites.copy() for i in range(3)]
+    b.reset()
+    assert b.state(0).sites.tobytes() == tumors[0].sites.tobytes()
+    b.set_doses(b.doses)
+    b.run(400)
+    ob = oracle.Batch(oracle.params_copy(params.native), 3, 99)
+    for i in range(3):
+        ob.set(i, tumors[0].sites, b.doses[0], epoch=1)
+    ob.run(400, nthreads=3)
+    _assert_same(b, ob, 3)
+    assert any(first[i].tobytes() != b.state(i).sites.tobytes() for i in range(3))
+
+
+def test_diffused_counter_matches_oracle(params, oracle):
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, 11, seed=4)]
+    st = np.zeros(2, np.int32)
+    sp = np.zeros(2, np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, [[]], st, sp, 300, seed=8)
+    assert b.diffused() == ob.diffused()
