@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Throughput of the EMT6-Ro batched simulation step on GB300.
+
+Workload (GA-scale uniform batch): 20 seeded disc tumours (radius 6-14 on the
+51 x 51 lattice) x 100 random 10-Gy protocols (1-8 doses, 0.25-Gy quanta,
+30-min grid in the first 48 h) x 20 replicates = 40,000 simulations, default
+parameters, 6-s steps.  One bench step advances every simulation by
+--sim-steps steps (default 600 = one simulated hour), continuing from the
+previous bench step.  Metric: site-updates/s = simulations x steps x 2601
+interior sites / time.
+
+  value          device time (CUDA events on the batch's stream) of the
+                 step kernels, state resident in HBM (7 GB >> 129 MB L2, so
+                 every launch streams its state from HBM; no flush needed)
+  e2e            the same through the public API (emt6ro.simulation
+                 .Experiment): per step add_irradiations (doses of that hour
+                 uploaded from the host), run, get_results (counts to host)
+  roofline       FP32 algorithmic flops of the dominant (narrow-region) step
+                 kernel against the device's measured FP32 FMA rate
+  cpu_baseline   the oracle port of the reference CPU path on the host cores,
+                 on a 64-simulation sample of the same workload
+
+--impl reference times that CPU path alone (all host threads).
+Under torchrun (--gpus N) every rank runs its own 40,000-simulation shard
+(weak scaling); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for p in (ROOT / "emt6-ro_gb300", ROOT):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+import numpy as np  # noqa: E402
+
+SITES = 51 * 51
+METRIC = "site-updates/s"
+FLOP_PER_SITE_SUBSTEP = 33  # 3 fields x 11 flop (9-point stencil + update)
+BYTES_PER_SITE_SUBSTEP = 24  # 3 fields x (4 B read + 4 B write)
+
+
+def shard_range(total: int, rank: int, world: int):
+    """Contiguous slice [lo, hi) of `total` units for `rank` of `world`."""
+    base, extra = divmod(total, world)
+    lo = rank * base + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
+
+
+def config1(n_reps: int = 20):
+    from emt6ro import workloads as wl
+    params = wl.default_parameters()
+    tumors = wl.tumors_config1(params, 20)
+    protocols = wl.protocols_config1(100)
+    T, P = len(tumors), len(protocols)
+    sim_tumor = np.repeat(np.tile(np.arange(T), P), n_reps).astype(np.int32)
+    sim_protocol = np.repeat(np.arange(P), T * n_reps).astype(np.int32)
+    return params, tumors, protocols, sim_tumor, sim_protocol
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms in the background."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def cpu_sample(params, tumors, protocols, sim_tumor, sim_protocol, steps, warmup, sim_steps,
+               n_sample=64, threads=None):
+    """The oracle port of the reference CPU path on a sample of the workload;
+    returns (site-updates/s per timed step list, threads)."""
+    from oracle import pyoracle as po
+    from emt6ro import workloads as wl
+    threads = threads or os.cpu_count() or 1
+    idx = np.linspace(0, len(sim_tumor) - 1, n_sample).astype(int)
+    doses = wl.protocol_doses(protocols, 480)
+    b = po.Batch(po.params_copy(params.native), n_sample, seed=1)
+    for k, i in enumerate(idx):
+        b.set(k, tumors[sim_tumor[i]].sites, doses[sim_protocol[i]], sim_index=int(i))
+    for _ in range(warmup):
+        b.run(sim_steps, nthreads=threads)
+    rates = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        b.run(sim_steps, nthreads=threads)
+        rates.append(n_sample * sim_steps * SITES / (time.perf_counter() - t))
+    return rates, threads, n_sample
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    params, tumors, protocols, st, sp = config1()
+    rates, threads, n = cpu_sample(params, tumors, protocols, st, sp, args.steps, args.warmup,
+                                   args.sim_steps)
+    v = statistics.median(rates)
+    ms = n * args.sim_steps * SITES / v * 1e3
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded disc tumours and protocols)",
+        "config": {"workload": "GA batch 20 tumours x 100 protocols x 20 runs, 53x53, 6-s "
+                               f"steps; CPU sample of {n} simulations x {args.sim_steps} steps",
+                   "sim_steps_per_step": args.sim_steps},
+        "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"{n} of the 40,000 simulations, {args.sim_steps} steps per "
+                                   "bench step, oracle/emt6_oracle.c restatement of the "
+                                   "reference CPU path, one simulation per thread"},
+        "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line
+
+
+def run_ours(args, rank, world, dist):
+    import ctypes
+    import torch
+    from emt6ro import _native as N
+    from emt6ro.batch import Batch
+    from emt6ro import simulation as sim
+    from emt6ro import workloads as wl
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    params, tumors, protocols, st, sp = config1()
+    B = len(st)
+    seed = 0xE6E6 + rank
+
+    # ---- device-resident run -------------------------------------------------
+    b = Batch(params, tumors, protocols, st, sp, device=dev, seed=seed)
+    b.set_schedule(0, args.sim_steps)
+    stream = torch.cuda.ExternalStream(b.stream())
+    for _ in range(args.warmup):
+        b.run(args.sim_steps)
+    b.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    d0, l0 = b.diffused(), b.launches()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        b.run(args.sim_steps)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    clocks.stop()
+    b.sync()
+    times = [s.elapsed_time(e) for s, e in ev]
+    total_ms = sum(times)
+    diffused = b.diffused() - d0
+    launches = b.launches() - l0
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * B * args.sim_steps * SITES / (ms_per_step * 1e-3)
+
+    # ---- end to end through the public API -----------------------------------
+    bins = (144_000 + 299) // 300
+    e2e_value = None
+    h2d = d2h = 0
+    exp = sim.Experiment(params, tumors, 20, len(protocols), gpu_id=dev, seed=seed)
+    for w in range(args.warmup):
+        exp.add_irradiations(_window(protocols, w, args.sim_steps))
+        exp.run(args.sim_steps)
+        exp.get_results()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        exp.add_irradiations(_window(protocols, args.warmup + k, args.sim_steps))
+        exp.run(args.sim_steps)
+        res = exp.get_results()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * B * args.sim_steps * SITES * args.steps / e2e_s
+    h2d = len(protocols) * bins * 4     # dose table upload per add_irradiations
+    d2h = int(res.size) * 4             # living counts per get_results
+    del exp
+
+    # ---- roofline of the dominant kernel -------------------------------------
+    peak = ctypes.c_double()
+    N.check(N.lib().emt6_probe_fp32_peak(dev, ctypes.byref(peak)))
+    kernel_ms = ms_per_step  # both step kernels of a bench step; the wide one has no work
+    achieved = diffused / args.steps * FLOP_PER_SITE_SUBSTEP / (kernel_ms * 1e-3) / 1e12
+    profiles = ROOT / "profiles" / "traffic.json"
+    traffic = None
+    if profiles.exists():
+        try:
+            traffic = json.loads(profiles.read_text()).get("dram_bytes_per_launch")
+        except ValueError:
+            traffic = None
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+            "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
+            "peak_source": "measured FP32 FMA rate of this GPU (emt6_probe_fp32_peak); "
+                           "MEASURED_PEAKS.json has no FP32 figure",
+            "algorithmic": f"{FLOP_PER_SITE_SUBSTEP} flop per diffused site-substep x "
+                           f"{diffused // args.steps} site-substeps per bench step"}
+    hbm_peak = _measured_hbm()
+    state_bytes = B * (3 * 2809 * 4 + 2809 + 2 * 2857) * 2
+    roof_hbm = {"bound": "hbm", "achieved": state_bytes / (kernel_ms * 1e-3) / 1e9,
+                "peak": hbm_peak, "unit": "GB/s",
+                "frac": state_bytes / (kernel_ms * 1e-3) / 1e9 / hbm_peak if hbm_peak else None,
+                "traffic": traffic,
+                "note": "resident design: each launch loads and stores each simulation's "
+                        "lattice once; per-step stencil traffic stays in registers/shared "
+                        f"memory ({BYTES_PER_SITE_SUBSTEP} B per site-substep on chip)"}
+    return {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded disc tumours and protocols, default parameters)",
+        "config": {"workload": "GA batch: 20 tumours x 100 protocols x 20 runs = 40,000 "
+                               "simulations per GPU, 53x53 lattice, 6-s steps",
+                   "sim_steps_per_step": args.sim_steps, "simulations_per_gpu": B,
+                   "l2": "state 7 GB per GPU >> 129 MB L2; no flush needed",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "roofline": roof,
+        "roofline_hbm": roof_hbm,
+        "diffused_site_substeps_per_step": diffused // args.steps,
+    }
+
+
+def _window(protocols, k, sim_steps):
+    """The (step, dose) pairs of each protocol falling in bench step k."""
+    lo, hi = k * sim_steps, (k + 1) * sim_steps
+    return [[(t, d) for t, d in prot if lo <= t < hi] for prot in protocols]
+
+
+def _measured_hbm():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"])
+        except (ValueError, KeyError):
+            pass
+    return 6800.0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--sim-steps", type=int, default=600)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        tdist.init_process_group(backend)
+        dist = tdist
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world, dist)
+        if rank == 0 and not args.no_cpu_baseline:
+            params, tumors, protocols, st, sp = config1()
+            rates, threads, n = cpu_sample(params, tumors, protocols, st, sp, 2, 1,
+                                           args.sim_steps)
+            line["cpu_baseline"] = {
+                "value": statistics.median(rates), "unit": METRIC, "cores": threads,
+                "kind": "port",
+                "sample": f"{n} of the 40,000 simulations x {args.sim_steps} steps, "
+                          "oracle/emt6_oracle.c restatement of the reference CPU path"}
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -59,7 +59,9 @@ __host__ __device__ inline SmemLayout smem_layout(int HW, int lcap, int np) {
   L.list = o; o += align_up((uint32_t)lcap * 2u, 16);
   L.aux = o; o += align_up((uint32_t)lcap, 16);
   L.colmask = o; o += 64 * 8;
-  L.xch = o; o += 3u * (uint32_t)np * 128u * 16u;
+  // boundary-row exchange: per field, 2 parities x NP parts x (1 side when
+  // NP == 2, else 2) x 32 lanes of float4
+  L.xch = o; o += 3u * 2u * (uint32_t)np * (np == 2 ? 1u : 2u) * 32u * 16u;
   L.misc = o; o += align_up(sizeof(Misc), 16);
   L.total = o;
   return L;
@@ -273,64 +275,108 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
     if (WIDE) x1[i] = (inr && j1 < ncol) ? (((fm1 >> i) & 1u) ? f[lat0 + gi * W + j1] : ext) : 0.f;
   }
 
-  // xch[(part * 2 + parity) * 64 + side * 32 + lane]; side 0 = first row, 1 = last row
+  // exchange slot of (parity, part, side); side 0 = the part's first row
+  // (read by part - 1), side 1 = its last row (read by part + 1)
+  auto slot = [&](int par, int pt, int side) -> float4 * {
+    return xch + (NP == 2 ? (par * 2 + pt) : ((par * NP + pt) * 2 + side)) * 32 + lane;
+  };
   for (int s = 0; s <= nfree; ++s) {
     const bool fin = (s == nfree);
     const uint32_t u0 = fin ? rm0 : fm0;
     const uint32_t u1 = fin ? rm1 : fm1;
     const int par = s & 1;
-    {
-      float ht0, ht1 = 0.f, hb0, hb1 = 0.f;
-      if (WIDE) {
-        ht0 = __shfl_sync(kFull, x1[0], left) + x1[0];
-        ht1 = x0[0] + __shfl_sync(kFull, x0[0], right);
-        hb0 = __shfl_sync(kFull, x1[RH - 1], left) + x1[RH - 1];
-        hb1 = x0[RH - 1] + __shfl_sync(kFull, x0[RH - 1], right);
-      } else {
-        ht0 = __shfl_sync(kFull, x0[0], left) + __shfl_sync(kFull, x0[0], right);
-        hb0 = __shfl_sync(kFull, x0[RH - 1], left) + __shfl_sync(kFull, x0[RH - 1], right);
-      }
-      float4 *mine = xch + (part * 2 + par) * 64 + lane;
-      if (part > 0) mine[0] = make_float4(x0[0], ht0, WIDE ? x1[0] : 0.f, ht1);
-      if (part < NP - 1) mine[32] = make_float4(x0[RH - 1], hb0, WIDE ? x1[RH - 1] : 0.f, hb1);
-    }
-    named_barrier(bar_id, NP * 32);
-    float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), nx = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (part > 0) pv = xch[((part - 1) * 2 + par) * 64 + 32 + lane];
-    if (part < NP - 1) nx = xch[((part + 1) * 2 + par) * 64 + lane];
-
-    float xm0 = pv.x, hm0 = pv.y, xm1 = pv.z, hm1 = pv.w;
-    float hc0, hc1 = 0.f;
-    if (WIDE) {
-      hc0 = __shfl_sync(kFull, x1[0], left) + x1[0];
-      hc1 = x0[0] + __shfl_sync(kFull, x0[0], right);
-    } else {
-      hc0 = __shfl_sync(kFull, x0[0], left) + __shfl_sync(kFull, x0[0], right);
-    }
+    if constexpr (!WIDE && RH <= 14) {
+      // all horizontal sums of the substep first: 2*RH independent shuffles
+      float h0[RH];
 #pragma unroll
-    for (int i = 0; i < RH; ++i) {
-      float xn0, hn0, xn1 = 0.f, hn1 = 0.f;
-      if (i + 1 < RH) {
-        xn0 = x0[i + 1];
-        if (WIDE) {
+      for (int i = 0; i < RH; ++i)
+        h0[i] = __shfl_sync(kFull, x0[i], left) + __shfl_sync(kFull, x0[i], right);
+      if (part > 0) *slot(par, part, 0) = make_float4(x0[0], h0[0], 0.f, 0.f);
+      if (part < NP - 1) *slot(par, part, 1) = make_float4(x0[RH - 1], h0[RH - 1], 0.f, 0.f);
+      named_barrier(bar_id, NP * 32);
+      float2 pv = make_float2(0.f, 0.f), nx = make_float2(0.f, 0.f);
+      if (part > 0) {
+        const float4 v = *slot(par, part - 1, 1);
+        pv = make_float2(v.x, v.y);
+      }
+      if (part < NP - 1) {
+        const float4 v = *slot(par, part + 1, 0);
+        nx = make_float2(v.x, v.y);
+      }
+      float xm0 = pv.x, hm0 = pv.y;
+#pragma unroll
+      for (int i = 0; i < RH; ++i) {
+        const float xn0 = (i + 1 < RH) ? x0[i + 1] : nx.x;
+        const float hn0 = (i + 1 < RH) ? h0[i + 1] : nx.y;
+        const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i] + (xm0 + xn0), cd * (hm0 + hn0)));
+        xm0 = x0[i];
+        if ((u0 >> i) & 1u) x0[i] = nv0;
+        hm0 = h0[i];
+      }
+    } else if constexpr (!WIDE) {
+      // RH = 16: horizontal sums on the fly (the two-phase form needs 16 more
+      // registers than the narrow kernel's budget)
+      const float ht0 = __shfl_sync(kFull, x0[0], left) + __shfl_sync(kFull, x0[0], right);
+      const float hb0 =
+          __shfl_sync(kFull, x0[RH - 1], left) + __shfl_sync(kFull, x0[RH - 1], right);
+      if (part > 0) *slot(par, part, 0) = make_float4(x0[0], ht0, 0.f, 0.f);
+      if (part < NP - 1) *slot(par, part, 1) = make_float4(x0[RH - 1], hb0, 0.f, 0.f);
+      named_barrier(bar_id, NP * 32);
+      float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), nx = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (part > 0) pv = *slot(par, part - 1, 1);
+      if (part < NP - 1) nx = *slot(par, part + 1, 0);
+      float xm0 = pv.x, hm0 = pv.y, hc0 = ht0;
+#pragma unroll
+      for (int i = 0; i < RH; ++i) {
+        float xn0, hn0;
+        if (i + 1 < RH) {
+          xn0 = x0[i + 1];
+          hn0 = __shfl_sync(kFull, xn0, left) + __shfl_sync(kFull, xn0, right);
+        } else {
+          xn0 = nx.x;
+          hn0 = nx.y;
+        }
+        const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0 + (xm0 + xn0), cd * (hm0 + hn0)));
+        xm0 = x0[i];
+        if ((u0 >> i) & 1u) x0[i] = nv0;
+        hm0 = hc0;
+        hc0 = hn0;
+      }
+    } else {
+      {
+        const float ht0 = __shfl_sync(kFull, x1[0], left) + x1[0];
+        const float ht1 = x0[0] + __shfl_sync(kFull, x0[0], right);
+        const float hb0 = __shfl_sync(kFull, x1[RH - 1], left) + x1[RH - 1];
+        const float hb1 = x0[RH - 1] + __shfl_sync(kFull, x0[RH - 1], right);
+        if (part > 0) *slot(par, part, 0) = make_float4(x0[0], ht0, x1[0], ht1);
+        if (part < NP - 1) *slot(par, part, 1) = make_float4(x0[RH - 1], hb0, x1[RH - 1], hb1);
+      }
+      named_barrier(bar_id, NP * 32);
+      float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), nx = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (part > 0) pv = *slot(par, part - 1, 1);
+      if (part < NP - 1) nx = *slot(par, part + 1, 0);
+      float xm0 = pv.x, hm0 = pv.y, xm1 = pv.z, hm1 = pv.w;
+      float hc0 = __shfl_sync(kFull, x1[0], left) + x1[0];
+      float hc1 = x0[0] + __shfl_sync(kFull, x0[0], right);
+#pragma unroll
+      for (int i = 0; i < RH; ++i) {
+        float xn0, hn0, xn1, hn1;
+        if (i + 1 < RH) {
+          xn0 = x0[i + 1];
           xn1 = x1[i + 1];
           hn0 = __shfl_sync(kFull, xn1, left) + xn1;
           hn1 = xn0 + __shfl_sync(kFull, xn0, right);
         } else {
-          hn0 = __shfl_sync(kFull, xn0, left) + __shfl_sync(kFull, xn0, right);
+          xn0 = nx.x; hn0 = nx.y; xn1 = nx.z; hn1 = nx.w;
         }
-      } else {
-        xn0 = nx.x; hn0 = nx.y; xn1 = nx.z; hn1 = nx.w;
-      }
-      const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0 + (xm0 + xn0), cd * (hm0 + hn0)));
-      xm0 = x0[i];
-      if ((u0 >> i) & 1u) x0[i] = nv0;
-      hm0 = hc0;
-      hc0 = hn0;
-      if (WIDE) {
+        const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0 + (xm0 + xn0), cd * (hm0 + hn0)));
         const float nv1 = fmaf(ca, x1[i], fmaf(cb, hc1 + (xm1 + xn1), cd * (hm1 + hn1)));
+        xm0 = x0[i];
         xm1 = x1[i];
+        if ((u0 >> i) & 1u) x0[i] = nv0;
         if ((u1 >> i) & 1u) x1[i] = nv1;
+        hm0 = hc0;
+        hc0 = hn0;
         hm1 = hc1;
         hc1 = hn1;
       }
@@ -360,7 +406,7 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
   int RH = (nrow + NP - 1) / NP;
   RH = (RH + 1) & ~1;
   float *f = fld + field * p.HW;
-  float4 *x = xch + field * NP * 128;
+  float4 *x = xch + field * 2 * NP * (NP == 2 ? 1 : 2) * 32;
   const float ext = p.ext[field], ca = p.da[field], cb = p.db[field], cd = p.dd[field];
   const int nf = p.nfree, bar = 1 + field, W = p.W;
 #define EMT6_CALL(R, WD)                                                                   \
@@ -573,6 +619,7 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
       __syncthreads();
 
       // ---- cell update (simulation.cu:84-96) ----
+      bool any_ready = false;
       const float dose =
           (t < p.length && t % p.res == 0 && t / p.res < p.bins) ? doses[t / p.res] : 0.f;
       for (uint32_t e = tid; e < n; e += NT) {
@@ -586,6 +633,7 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
         const bool ready = step_site(p, fld, st, cells, s, aux[e], dose, t, (uint32_t)sim, 0,
                                      a.epoch, m);
         aux[e] = ready ? 0x80 : 0;
+        any_ready |= ready;
       }
       if (m->has_multi && wid == 0) {
         // sites listed more than once: every entry steps the site, in list order
@@ -608,6 +656,7 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
                 if (ready) {
                   if (occ > 127) atomicOr(a.err, 4u);
                   res = (uint8_t)(0x80 | (occ & 0x7f));
+                  any_ready = true;
                 }
               }
               aux[ee] = res;
@@ -616,7 +665,8 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
           }
         }
       }
-      __syncthreads();
+      // most steps have no cell ready to divide: skip the arbitration then
+      if (!__syncthreads_or(any_ready)) continue;
 
       // ---- division arbitration: lowest list index with a vacant target ----
       int best = 0x7fffffff, best_target = -1;
@@ -929,6 +979,51 @@ cudaError_t instr_reset() {
   e = cudaMemcpyToSymbol(g_instr_sum_death_prob, &zd, sizeof(double));
   if (e != cudaSuccess) return e;
   return cudaMemcpyToSymbol(g_instr_hist, z, sizeof(z));
+}
+
+// FP32 issue-rate probe: 8 independent FMA chains per thread, register only
+__global__ void __launch_bounds__(256) fma_probe_kernel(float *out, float a, float b, int iters) {
+  float x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = a * (threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], b, a);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 1234.5f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+cudaError_t fp32_peak(int device, double *tflops) {
+  int sms = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return e;
+  const int blocks = sms * 8, threads = 256, iters = 8192;
+  float *out = nullptr;
+  e = cudaMalloc(&out, sizeof(float) * blocks * threads);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  double best = 0;
+  for (int rep = 0; rep < 12; ++rep) {
+    cudaEventRecord(t0);
+    fma_probe_kernel<<<blocks, threads>>>(out, 1.0001f, 0.9999f, iters);
+    cudaEventRecord(t1);
+    e = cudaEventSynchronize(t1);
+    if (e != cudaSuccess) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t0, t1);
+    const double flop = 2.0 * 8 * (double)iters * blocks * threads;
+    if (rep >= 2 && ms > 0) best = fmax(best, flop / (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(out);
+  *tflops = best;
+  return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 cudaError_t launch_test_philox(const uint4 *c, const uint2 *k, uint4 *o, int64_t n) {

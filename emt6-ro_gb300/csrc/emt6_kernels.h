@@ -61,6 +61,7 @@ cudaError_t launch_run(const RunArgs &a, uint32_t t_end, bool wide, int grid,
 cudaError_t launch_reset(const ResetArgs &a, cudaStream_t stream);
 cudaError_t instr_read(unsigned long long counts[4], double *sum_dp, unsigned long long *hist);
 cudaError_t instr_reset();
+cudaError_t fp32_peak(int device, double *tflops);
 
 cudaError_t launch_test_philox(const uint4 *c, const uint2 *k, uint4 *o, int64_t n);
 cudaError_t launch_test_math(const float *x, float *ex, const double *u, double *lg, double *sn,

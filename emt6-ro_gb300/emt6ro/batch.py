@@ -85,6 +85,11 @@ class Batch:
         N.check(N.lib().emt6_batch_diffused(self._h, ctypes.byref(v)))
         return int(v.value)
 
+    def launches(self) -> int:
+        v = ctypes.c_ulonglong()
+        N.check(N.lib().emt6_batch_launches(self._h, ctypes.byref(v)))
+        return int(v.value)
+
     def stream(self) -> int:
         return int(N.lib().emt6_batch_stream(self._h) or 0)
 
