@@ -287,6 +287,7 @@ struct emt6_batch {
   uint64_t seed = 0;
   int sched = 0;
   uint32_t chunk = 1200;
+  unsigned long long launches = 0;  // kernels issued by this handle
   bool has_horizon = false;
   uint32_t max_horizon = 0xFFFFFFFFu;
   DevBuf<float> fld, tpl_fld, doses;
@@ -371,6 +372,7 @@ struct emt6_batch {
     r.HW = HW;
     r.nsims = n;
     EMT6_CUDA(emt6::launch_reset(r, stream));
+    launches += 1;
     std::fill(h_doses.begin(), h_doses.end(), 0.f);
     int rc = upload_doses();
     if (rc) return rc;
@@ -400,6 +402,7 @@ struct emt6_batch {
           a.queue = 1;
         }
         EMT6_CUDA(emt6::launch_run(a, end, wide != 0, grid, stream));
+        launches += 1;
       }
       t_host = end;
     }
@@ -782,6 +785,7 @@ int emt6_batch_counts(emt6_batch *b, uint32_t *out) {
   const int grid = (int)std::min<int64_t>(b->n, 65535 * 4);
   count_kernel<<<grid, 256, 0, b->stream>>>(b->st.p, b->sstride, b->HW, b->counts.p, b->n);
   EMT6_CUDA(cudaGetLastError());
+  b->launches += 1;
   EMT6_CUDA(cudaMemcpyAsync(out, b->counts.p, b->n * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             b->stream));
   EMT6_CUDA(cudaStreamSynchronize(b->stream));
@@ -827,6 +831,21 @@ int emt6_batch_diffused(emt6_batch *b, unsigned long long *out) {
   DeviceGuard g(b->device);
   EMT6_CUDA(cudaMemcpyAsync(out, b->diffused.p, 8, cudaMemcpyDeviceToHost, b->stream));
   EMT6_CUDA(cudaStreamSynchronize(b->stream));
+  return EMT6_OK;
+}
+
+int emt6_batch_launches(emt6_batch *b, unsigned long long *out) {
+  if (!b || !out) return fail(EMT6_ERR_INVALID, "null argument");
+  *out = b->launches;
+  return EMT6_OK;
+}
+
+int emt6_probe_fp32_peak(int32_t device, double *tflops) {
+  if (!tflops) return fail(EMT6_ERR_INVALID, "null argument");
+  DeviceGuard g(device);
+  double best = 0;
+  EMT6_CUDA(emt6::fp32_peak(device, &best));
+  *tflops = best;
   return EMT6_OK;
 }
 
@@ -1153,3 +1172,4 @@ int emt6_test_diffuse(const emt6_params *p, float *fields, int32_t height, int32
 }
 
 }  // extern "C"
+

@@ -16,6 +16,7 @@ _LIB_PATH = _PKG / "_lib" / "libemt6ro_gb300.so"
 
 EMT6_OK = 0
 EMT6_ERR_STATE = 3
+EMT6_ERR_LIMIT = 5
 MAX_INTERIOR_HEIGHT = 54
 MAX_INTERIOR_WIDTH = 60
 INSTR_HIST_N = 300
@@ -82,6 +83,8 @@ _SIGNATURES = {
     "emt6_batch_stream": (_VP, [_VP]),
     "emt6_batch_diffused": (_c.c_int, [_VP, _P(_c.c_ulonglong)]),
     "emt6_batch_set_schedule": (_c.c_int, [_VP, _c.c_int32, _c.c_uint32]),
+    "emt6_batch_launches": (_c.c_int, [_VP, _P(_c.c_ulonglong)]),
+    "emt6_probe_fp32_peak": (_c.c_int, [_c.c_int32, _P(_c.c_double)]),
     "emt6_experiment_create": (_c.c_int, [_P(Params), _VP, _c.c_int32, _c.c_int32, _c.c_int32,
                                           _c.c_int32, _c.c_int32, _c.c_uint32, _c.c_uint32,
                                           _c.c_int32, _c.c_uint64, _P(_VP)]),

@@ -125,6 +125,11 @@ int emt6_batch_step(emt6_batch *b, int64_t sim, uint32_t *out);
 void *emt6_batch_stream(emt6_batch *b);
 /* Diffused site-substeps executed since creation (for throughput accounting). */
 int emt6_batch_diffused(emt6_batch *b, unsigned long long *out);
+/* Kernels this handle has launched since creation (run, reset, count). */
+int emt6_batch_launches(emt6_batch *b, unsigned long long *out);
+/* Measured FP32 FMA throughput of the device (TFLOP/s): the ceiling the
+ * FP32 stencil is reported against. No reference counterpart. */
+int emt6_probe_fp32_peak(int32_t device, double *tflops);
 /* Sims per CTA scheduling: 0 = one CTA per simulation (default), 1 = persistent
  * CTAs over a device work queue ordered by longest horizon first. */
 int emt6_batch_set_schedule(emt6_batch *b, int32_t mode, uint32_t steps_per_launch);
