@@ -21,7 +21,7 @@ INCLUDE = HERE.parent / "include"
 OUT_DIR = HERE / "emt6ro" / "_lib"
 LIB = OUT_DIR / "libemt6ro_gb300.so"
 OBJ_DIR = HERE / "_build"
-SOURCES = ["emt6_kernels.cu", "emt6_host.cu"]
+SOURCES = ["emt6_kernels.cu", "emt6_host.cu", "emt6_noalloc.cu"]
 HEADERS = ["emt6_device.cuh", "emt6_kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",

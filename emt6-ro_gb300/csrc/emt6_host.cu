@@ -1173,3 +1173,11 @@ int emt6_test_diffuse(const emt6_params *p, float *fields, int32_t height, int32
 
 }  // extern "C"
 
+namespace emt6 {
+// for the allocation-free entry point (emt6_noalloc.cu)
+KParams make_kparams_public(const emt6_params &p, uint64_t seed, uint32_t res, uint32_t length,
+                            uint32_t bins) {
+  return make_kparams(p, seed, res, length, bins);
+}
+int set_error(int code, const std::string &msg) { return fail(code, msg); }
+}  // namespace emt6
