@@ -288,6 +288,54 @@ def run_ours(args, rank, world, dist):
     }
 
 
+def run_config2(args):
+    """Ragged batch: 30,000 simulations, disc radius 2-20, 0-12 doses, horizons
+    {72k, 144k, 288k} steps (5, 10, 20 days) mixed uniformly, scaled by
+    --horizon-scale; launch schedule chosen by the autotuner; reports the
+    makespan (tail latency of the slowest simulation) and site-updates/s."""
+    import torch
+    from emt6ro import workloads as wl, autotune
+    from emt6ro.batch import Batch
+    params = wl.default_parameters()
+    tumors, prots, st, sp, hz = wl.ragged_config2(params, 30_000)
+    hz = np.maximum((hz.astype(np.float64) * args.horizon_scale).astype(np.uint32), 1)
+    t0 = time.perf_counter()
+    mode, chunk, table = autotune.tune(params, tumors, prots, st, sp, hz, sample=2432,
+                                       trial_steps=min(600, int(hz.min())))
+    tune_s = time.perf_counter() - t0
+    b = Batch(params, tumors, prots, st, sp, sim_horizon=hz, seed=0xC0FFEE)
+    b.set_schedule(mode, chunk)
+    stream = torch.cuda.ExternalStream(b.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    clocks.start()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    b.run(int(hz.max()))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks.stop()
+    b.sync()
+    ms = e0.elapsed_time(e1)
+    work = float(hz.astype(np.float64).sum()) * SITES
+    steps_done = [b.step(i) for i in range(0, len(st), 997)]
+    assert all(s == int(hz[i]) for s, i in zip(steps_done, range(0, len(st), 997)))
+    return {
+        "metric": METRIC, "value": work / (ms * 1e-3), "unit": METRIC, "n_gpus": 1,
+        "steps": 1, "warmup": 0, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ragged batch)",
+        "config": {"workload": "ragged batch: 30,000 simulations, disc radius 2-20, 0-12 doses, "
+                               "horizons 5/10/20 days mixed",
+                   "horizon_scale": args.horizon_scale,
+                   "horizons_steps": sorted({int(x) for x in np.unique(hz)}),
+                   "schedule_mode": mode, "steps_per_launch": chunk},
+        "tail_latency_s": ms * 1e-3,
+        "autotune": {"seconds": tune_s, "table": [[m, c, round(t, 4)] for m, c, t in table]},
+        "clocks": clocks.summary(), "gpu_launches": b.launches(),
+    }
+
+
 def _window(protocols, k, sim_steps):
     """The (step, dose) pairs of each protocol falling in bench step k."""
     lo, hi = k * sim_steps, (k + 1) * sim_steps
@@ -312,7 +360,14 @@ def main():
     ap.add_argument("--sim-steps", type=int, default=600)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", type=int, choices=[1, 2], default=1,
+                    help="1: GA batch (default, the headline); 2: ragged batch")
+    ap.add_argument("--horizon-scale", type=float, default=1.0,
+                    help="config 2: multiply the 72k/144k/288k-step horizons")
     args = ap.parse_args()
+    if args.config == 2:
+        print(json.dumps(run_config2(args)), flush=True)
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     dist = None

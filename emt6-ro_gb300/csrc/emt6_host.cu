@@ -288,6 +288,12 @@ struct emt6_batch {
   int sched = 0;
   uint32_t chunk = 1200;
   unsigned long long launches = 0;  // kernels issued by this handle
+  bool use_graph = false;
+  bool occ_known = false;
+  int per_sm_cache[2] = {1, 1};
+  cudaGraphExec_t graph_exec = nullptr;
+  uint64_t graph_key[5] = {0, 0, 0, 0, 0};
+  unsigned long long graph_kernels = 0;
   bool has_horizon = false;
   uint32_t max_horizon = 0xFFFFFFFFu;
   DevBuf<float> fld, tpl_fld, doses;
@@ -305,6 +311,7 @@ struct emt6_batch {
     if (stream) {
       DeviceGuard g(device);
       cudaStreamSynchronize(stream);
+      if (graph_exec) cudaGraphExecDestroy(graph_exec);
       cudaStreamDestroy(stream);
     }
   }
@@ -381,31 +388,78 @@ struct emt6_batch {
     return EMT6_OK;
   }
 
-  int run(uint32_t nsteps) {
-    const uint64_t target64 = (uint64_t)t_host + nsteps;
-    const uint32_t target = target64 > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)target64;
+  // launches of one run() call from t_host to target, on the handle's stream
+  int issue(uint32_t target, unsigned long long *count) {
     emt6::RunArgs a = run_args();
     int sms = 0;
     EMT6_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    while (t_host < target) {
-      uint32_t end = std::min<uint64_t>(target, (uint64_t)t_host + chunk);
-      if (has_horizon && t_host >= max_horizon) {
-        t_host = target;
-        break;
-      }
+    if (!occ_known) {
+      for (int wide = 0; wide < 2; ++wide)
+        per_sm_cache[wide] = std::max(emt6::max_ctas_per_sm(kp, wide != 0), 1);
+      occ_known = true;
+    }
+    const int *per_sm = per_sm_cache;
+    uint32_t t = t_host;
+    while (t < target) {
+      const uint32_t end = (uint32_t)std::min<uint64_t>(target, (uint64_t)t + chunk);
+      if (has_horizon && t >= max_horizon) break;
       for (int wide = 0; wide < 2; ++wide) {
         int grid = (int)std::min<int64_t>(n, 0x7fffffff);
         if (sched == 1) {
-          const int per_sm = emt6::max_ctas_per_sm(kp, wide != 0);
-          grid = (int)std::min<int64_t>(n, (int64_t)std::max(per_sm, 1) * sms);
+          grid = (int)std::min<int64_t>(n, (int64_t)per_sm[wide] * sms);
           EMT6_CUDA(cudaMemsetAsync(ticket.p, 0, sizeof(uint32_t), stream));
           a.queue = 1;
         }
         EMT6_CUDA(emt6::launch_run(a, end, wide != 0, grid, stream));
-        launches += 1;
+        *count += 1;
       }
-      t_host = end;
+      t = end;
     }
+    return EMT6_OK;
+  }
+
+  int run(uint32_t nsteps) {
+    const uint64_t target64 = (uint64_t)t_host + nsteps;
+    const uint32_t target = target64 > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)target64;
+    if (!use_graph) {
+      int rc = issue(target, &launches);
+      if (rc) return rc;
+      t_host = target;
+      return EMT6_OK;
+    }
+    // CUDA-graph mode: capture the whole chunk sequence once per
+    // (start, target, schedule, chunk, epoch) and replay it
+    const uint64_t key[5] = {t_host, target, (uint64_t)sched, chunk, epoch};
+    if (!graph_exec || std::memcmp(key, graph_key, sizeof(key)) != 0) {
+      if (graph_exec) {
+        cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+      }
+      // occupancy queries and attributes outside the capture
+      if (!occ_known) {
+        for (int wide = 0; wide < 2; ++wide)
+          per_sm_cache[wide] = std::max(emt6::max_ctas_per_sm(kp, wide != 0), 1);
+        occ_known = true;
+      }
+      EMT6_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      unsigned long long nodes = 0;
+      int rc = issue(target, &nodes);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(stream, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (e != cudaSuccess) return fail(EMT6_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&graph_exec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return fail(EMT6_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+      std::memcpy(graph_key, key, sizeof(key));
+      graph_kernels = nodes;
+    }
+    EMT6_CUDA(cudaGraphLaunch(graph_exec, stream));
+    launches += graph_kernels;
+    t_host = target;
     return EMT6_OK;
   }
 };
@@ -850,9 +904,10 @@ int emt6_probe_fp32_peak(int32_t device, double *tflops) {
 }
 
 int emt6_batch_set_schedule(emt6_batch *b, int32_t mode, uint32_t steps_per_launch) {
-  if (!b || mode < 0 || mode > 1) return fail(EMT6_ERR_INVALID, "bad schedule");
+  if (!b || mode < 0 || mode > 3) return fail(EMT6_ERR_INVALID, "bad schedule");
   std::lock_guard<std::mutex> lk(b->mu);
-  b->sched = mode;
+  b->sched = mode & 1;
+  b->use_graph = (mode & 2) != 0;
   if (steps_per_launch) b->chunk = steps_per_launch;
   return EMT6_OK;
 }
@@ -1141,6 +1196,9 @@ static int test_block(int mode, int variant, const emt6_params *pp, float *field
     if (roi[2] > 0)
       EMT6_CUDA(cudaMemcpy(mask, dm.p, (roi[2] + 2) * (roi[3] + 2), cudaMemcpyDeviceToHost));
   } else {
+    uint32_t refused = 0;
+    EMT6_CUDA(cudaMemcpy(&refused, dn.p, 4, cudaMemcpyDeviceToHost));
+    if (refused) return fail(EMT6_ERR_LIMIT, "region does not fit the narrow kernel path");
     EMT6_CUDA(cudaMemcpy(fields, df.p, 3 * HW * 4, cudaMemcpyDeviceToHost));
   }
   return EMT6_OK;
@@ -1163,9 +1221,6 @@ int emt6_test_list(const uint8_t *state, int32_t height, int32_t width, uint16_t
 int emt6_test_diffuse(const emt6_params *p, float *fields, int32_t height, int32_t width,
                       const int32_t *roi, int32_t variant, int32_t device) {
   if (!p || !fields || !roi) return fail(EMT6_ERR_INVALID, "null argument");
-  const int nrow = roi[2] + 2, ncol = roi[3] + 2;
-  if (variant == 0 && (nrow > 32 || ncol > 31))
-    return fail(EMT6_ERR_LIMIT, "region too large for the narrow kernel path");
   int32_t r[8] = {roi[0], roi[1], roi[2], roi[3], roi[4], 0, 0, 0};
   return test_block(2, variant, p, fields, nullptr, height, width, r, nullptr, nullptr, nullptr,
                     device);

@@ -41,6 +41,7 @@ struct Misc {
   double ins_dp;
   unsigned long long diffused;
   unsigned long long nfs;  // free sites of the current mask
+  int narrow_ok, roff, coff;  // region fits the narrow kernel; row/column offset
 };
 
 __host__ __device__ inline uint32_t align_up(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
@@ -238,6 +239,37 @@ __device__ void restore_colmask(uint64_t *colmask, const Misc *m) {
   }
 }
 
+// The narrow kernel maps lanes to 32 region columns and registers to at most
+// 32 region rows.  A 33-wide region fits when its ring columns 0 and 32 are
+// entirely fixed (an unclipped ROI): lanes then hold columns 1..32, and the
+// rotating shuffle hands lane 0 the value of column 32, which equals that of
+// column 0 (both fixed at the external level).  Likewise a 33-high region with
+// an entirely fixed first row holds rows 1..32; row 0 becomes a constant.
+// Called by one thread.
+__device__ void narrow_mapping(const uint64_t *colmask, Misc *m) {
+  const int nrow = m->roi[2] + 2, ncol = m->roi[3] + 2;
+  int ok = 1, roff = 0, coff = 0;
+  if (m->roi[2] == 0 || m->roi[3] == 0) {
+    ok = 1;
+  } else if (ncol > 33 || nrow > 33) {
+    ok = 0;
+  } else {
+    if (ncol == 33) {
+      if (colmask[0] != 0 || colmask[32] != 0) ok = 0;
+      coff = 1;
+    }
+    if (nrow == 33) {
+      uint64_t first = 0;
+      for (int j = 0; j < ncol; ++j) first |= colmask[j] & 1ull;
+      if (first) ok = 0;
+      roff = 1;
+    }
+  }
+  m->narrow_ok = ok;
+  m->roff = roff;
+  m->coff = coff;
+}
+
 // ---------------------------------------------------------------------------
 // diffusion of one field by one warp of NP (part k = region rows
 // [k*RH, (k+1)*RH) of the (h+2) x (w+2) region; lane = column, or columns
@@ -248,14 +280,20 @@ __device__ __forceinline__ void named_barrier(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
+// producer side of a named barrier: marks arrival without waiting
+__device__ __forceinline__ void named_arrive(int id, int n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
 template <int NP, int RH, bool WIDE>
 __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t *__restrict__ colmask,
                                           float4 *__restrict__ xch, int part, int r0, int c0,
                                           int h, int w, int nrow, int ncol, int W, float ext,
-                                          float ca, float cb, float cd, int nfree, int bar_id) {
+                                          float ca, float cb, float cd, int nfree, int bar_id,
+                                          int roff, int coff) {
   const int lane = threadIdx.x & 31;
-  const int base = part * RH;
-  const int j0 = WIDE ? 2 * lane : lane;
+  const int base = part * RH + roff;  // region row of register row 0
+  const int j0 = (WIDE ? 2 * lane : lane) + coff;
   const int j1 = 2 * lane + 1;
   const int left = (lane + 31) & 31, right = (lane + 1) & 31;
   const uint32_t rowsel = (1u << RH) - 1u;
@@ -265,6 +303,13 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
   const uint32_t rm0 = (j0 >= 1 && j0 <= w) ? roirows : 0u;
   const uint32_t rm1 = (WIDE && j1 >= 1 && j1 <= w) ? roirows : 0u;
   const int lat0 = (r0 - 1) * W + (c0 - 1);
+  // the row above part 0: the zero ring, or region row 0 held at the external
+  // level when the mapping starts at row 1 (evaluated where used)
+  auto top_x = [&]() -> float { return (roff && j0 < ncol) ? ext : 0.f; };
+  auto top_h = [&]() -> float {
+    return roff ? ((j0 - 1 >= 0 && j0 - 1 < ncol) ? ext : 0.f) + ((j0 + 1 < ncol) ? ext : 0.f)
+                : 0.f;
+  };
 
   float x0[RH], x1[WIDE ? RH : 1];
 #pragma unroll
@@ -285,33 +330,55 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
     const uint32_t u0 = fin ? rm0 : fm0;
     const uint32_t u1 = fin ? rm1 : fm1;
     const int par = s & 1;
-    if constexpr (!WIDE && RH <= 14) {
+    if constexpr (NP == 2 && !WIDE && RH <= 14) {
       // all horizontal sums of the substep first: 2*RH independent shuffles
       float h0[RH];
 #pragma unroll
       for (int i = 0; i < RH; ++i)
         h0[i] = __shfl_sync(kFull, x0[i], left) + __shfl_sync(kFull, x0[i], right);
-      if (part > 0) *slot(par, part, 0) = make_float4(x0[0], h0[0], 0.f, 0.f);
-      if (part < NP - 1) *slot(par, part, 1) = make_float4(x0[RH - 1], h0[RH - 1], 0.f, 0.f);
-      named_barrier(bar_id, NP * 32);
-      float2 pv = make_float2(0.f, 0.f), nx = make_float2(0.f, 0.f);
-      if (part > 0) {
-        const float4 v = *slot(par, part - 1, 1);
-        pv = make_float2(v.x, v.y);
-      }
-      if (part < NP - 1) {
-        const float4 v = *slot(par, part + 1, 0);
-        nx = make_float2(v.x, v.y);
-      }
-      float xm0 = pv.x, hm0 = pv.y;
+      // Producer/consumer exchange with the partner warp: publish the boundary
+      // row, arrive on this part's barrier, update every row that does not
+      // need the partner, then wait on the partner's barrier for its row.
+      // Barrier ids alternate with the substep parity so a warp that runs a
+      // substep ahead never arrives twice on one barrier instance.
+      const int own = bar_id + par * 2 + part, other = bar_id + par * 2 + (1 - part);
+      if (part == 0) {
+        *slot(par, 0, 1) = make_float4(x0[RH - 1], h0[RH - 1], 0.f, 0.f);
+        named_arrive(own, 64);
+        float xm0 = top_x(), hm0 = top_h();
 #pragma unroll
-      for (int i = 0; i < RH; ++i) {
-        const float xn0 = (i + 1 < RH) ? x0[i + 1] : nx.x;
-        const float hn0 = (i + 1 < RH) ? h0[i + 1] : nx.y;
-        const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i] + (xm0 + xn0), cd * (hm0 + hn0)));
-        xm0 = x0[i];
-        if ((u0 >> i) & 1u) x0[i] = nv0;
-        hm0 = h0[i];
+        for (int i = 0; i < RH - 1; ++i) {
+          const float nv0 =
+              fmaf(ca, x0[i], fmaf(cb, h0[i] + (xm0 + x0[i + 1]), cd * (hm0 + h0[i + 1])));
+          xm0 = x0[i];
+          if ((u0 >> i) & 1u) x0[i] = nv0;
+          hm0 = h0[i];
+        }
+        named_barrier(other, 64);
+        const float4 nx = *slot(par, 1, 0);
+        const float nv0 =
+            fmaf(ca, x0[RH - 1], fmaf(cb, h0[RH - 1] + (xm0 + nx.x), cd * (hm0 + nx.y)));
+        if ((u0 >> (RH - 1)) & 1u) x0[RH - 1] = nv0;
+      } else {
+        *slot(par, 1, 0) = make_float4(x0[0], h0[0], 0.f, 0.f);
+        named_arrive(own, 64);
+        const float x_first = x0[0], x_second = RH > 1 ? x0[1] : 0.f;
+        float xm0 = x0[0], hm0 = h0[0];
+#pragma unroll
+        for (int i = 1; i < RH; ++i) {
+          const float xn0 = (i + 1 < RH) ? x0[i + 1] : 0.f;
+          const float hn0 = (i + 1 < RH) ? h0[i + 1] : 0.f;
+          const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i] + (xm0 + xn0), cd * (hm0 + hn0)));
+          xm0 = x0[i];
+          if ((u0 >> i) & 1u) x0[i] = nv0;
+          hm0 = h0[i];
+        }
+        named_barrier(other, 64);
+        const float4 pv = *slot(par, 0, 1);
+        const float hn0 = RH > 1 ? h0[1] : 0.f;
+        const float nv0 =
+            fmaf(ca, x_first, fmaf(cb, h0[0] + (pv.x + x_second), cd * (pv.y + hn0)));
+        if (u0 & 1u) x0[0] = nv0;
       }
     } else if constexpr (!WIDE) {
       // RH = 16: horizontal sums on the fly (the two-phase form needs 16 more
@@ -324,6 +391,7 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
       named_barrier(bar_id, NP * 32);
       float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), nx = make_float4(0.f, 0.f, 0.f, 0.f);
       if (part > 0) pv = *slot(par, part - 1, 1);
+      else pv = make_float4(top_x(), top_h(), 0.f, 0.f);
       if (part < NP - 1) nx = *slot(par, part + 1, 0);
       float xm0 = pv.x, hm0 = pv.y, hc0 = ht0;
 #pragma unroll
@@ -403,15 +471,18 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
   const int nrow = h + 2, ncol = w + 2;
   const int wid = threadIdx.x >> 5;
   const int field = wid / NP, part = wid % NP;
-  int RH = (nrow + NP - 1) / NP;
+  const int roff = NP == 2 ? m->roff : 0, coff = NP == 2 ? m->coff : 0;
+  int RH = (nrow - roff + NP - 1) / NP;
   RH = (RH + 1) & ~1;
   float *f = fld + field * p.HW;
   float4 *x = xch + field * 2 * NP * (NP == 2 ? 1 : 2) * 32;
   const float ext = p.ext[field], ca = p.da[field], cb = p.db[field], cd = p.dd[field];
-  const int nf = p.nfree, bar = 1 + field, W = p.W;
+  // named barriers: 4 ids per field in the two-warp path (2 parts x 2
+  // parities), one id per field otherwise; id 0 is __syncthreads
+  const int nf = p.nfree, bar = 1 + (NP == 2 ? 4 : 1) * field, W = p.W;
 #define EMT6_CALL(R, WD)                                                                   \
   diffuse_part<NP, R, WD>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, \
-                          nf, bar)
+                          nf, bar, roff, coff)
 #define EMT6_CASES(WD)                   \
   switch (RH) {                          \
     case 2: EMT6_CALL(2, WD); break;     \
@@ -432,6 +503,7 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
   } else {
     EMT6_CASES(WIDE_OK)
   }
+  (void)coff;
 #undef EMT6_CASES
 #undef EMT6_CALL
 }
@@ -576,6 +648,7 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
       unsigned long long nf = 0;
       for (int j = 0; j < 64; ++j) nf += __popcll(colmask[j]);
       m->nfs = nf;
+      narrow_mapping(colmask, m);
     }
     float4 *cells = a.cell + sim * (int64_t)HW * 3;
     const uint32_t step0 = a.step[sim];
@@ -594,12 +667,14 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
           unsigned long long nf = 0;
           for (int j = 0; j < 64; ++j) nf += __popcll(colmask[j]);
           m->nfs = nf;
+          narrow_mapping(colmask, m);
         }
+        __syncthreads();
       }
-      // a region wider than 31 columns is left for the wide-capable kernel;
-      // the state stored is the state at the start of step t (the list
+      // a region the narrow mapping cannot hold is left for the wide-capable
+      // kernel; the state stored is the state at the start of step t (the list
       // rebuild and ROI above are recomputed identically there)
-      if (!WIDE_OK && (m->roi[3] + 2 > 31 || m->roi[2] + 2 > 32)) break;
+      if (!WIDE_OK && !m->narrow_ok) break;
       // vacancy snapshot (simulation.cu:79-83), before any site changes
       const uint32_t n = m->n;
       for (uint32_t e = tid; e < n; e += NT) {
@@ -911,6 +986,13 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192)
     __syncthreads();
     restore_colmask(colmask, m);
     __syncthreads();
+    if (threadIdx.x == 0) {
+      narrow_mapping(colmask, m);
+      if (WIDE_OK) m->roff = m->coff = 0;
+      *gn = (WIDE_OK || m->narrow_ok) ? 0u : 1u;
+    }
+    __syncthreads();
+    if (!WIDE_OK && !m->narrow_ok) return;
     diffuse_step<NP, WIDE_OK>(fld, colmask, xch, m, p);
     __syncthreads();
     for (int q = threadIdx.x; q < 3 * HW; q += NT) gfld[q] = fld[q];
@@ -920,21 +1002,33 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192)
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
+// the dynamic shared-memory limit is raised once per device and size (the
+// attribute call is kept out of CUDA-graph captures)
+static size_t g_smem_set[2][64];
+
+static cudaError_t ensure_smem(bool wide, size_t smem) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) dev = 63;
+  if (g_smem_set[wide][dev] >= smem) return cudaSuccess;
+  e = wide ? cudaFuncSetAttribute(run_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem)
+           : cudaFuncSetAttribute(run_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem);
+  if (e == cudaSuccess) g_smem_set[wide][dev] = smem;
+  return e;
+}
+
 cudaError_t launch_run(const RunArgs &a, uint32_t t_end, bool wide, int grid,
                        cudaStream_t stream) {
   const size_t smem = run_kernel_smem(a.p.HW, a.p.lcap, wide);
-  cudaError_t e;
-  if (wide) {
-    e = cudaFuncSetAttribute(run_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
+  cudaError_t e = ensure_smem(wide, smem);
+  if (e != cudaSuccess) return e;
+  if (wide)
     run_kernel<true><<<grid, 384, smem, stream>>>(a, t_end);
-  } else {
-    e = cudaFuncSetAttribute(run_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
+  else
     run_kernel<false><<<grid, 192, smem, stream>>>(a, t_end);
-  }
   return cudaGetLastError();
 }
 
@@ -948,13 +1042,12 @@ cudaError_t launch_reset(const ResetArgs &a, cudaStream_t stream) {
 int max_ctas_per_sm(const KParams &p, bool wide) {
   const size_t smem = run_kernel_smem(p.HW, p.lcap, wide);
   int n = 0;
+  if (ensure_smem(wide, smem) != cudaSuccess) return 0;
   if (wide) {
-    cudaFuncSetAttribute(run_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, run_kernel<true>, 384, smem) !=
         cudaSuccess)
       return 0;
   } else {
-    cudaFuncSetAttribute(run_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, run_kernel<false>, 192, smem) !=
         cudaSuccess)
       return 0;

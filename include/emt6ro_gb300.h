@@ -130,8 +130,12 @@ int emt6_batch_launches(emt6_batch *b, unsigned long long *out);
 /* Measured FP32 FMA throughput of the device (TFLOP/s): the ceiling the
  * FP32 stencil is reported against. No reference counterpart. */
 int emt6_probe_fp32_peak(int32_t device, double *tflops);
-/* Sims per CTA scheduling: 0 = one CTA per simulation (default), 1 = persistent
- * CTAs over a device work queue ordered by longest horizon first. */
+/* Scheduling of emt6_batch_run.  mode bit 0: 0 = one CTA per simulation
+ * (default), 1 = persistent CTAs taking simulations from a device work queue
+ * ordered longest horizon first; bit 1: capture the run's launch sequence in
+ * a CUDA graph and replay it (re-captured when start step, target, schedule,
+ * chunk or epoch change).  steps_per_launch: steps per kernel launch (0 keeps
+ * the current value, default 1200). */
 int emt6_batch_set_schedule(emt6_batch *b, int32_t mode, uint32_t steps_per_launch);
 
 /* ---- Experiment: protocols x tumours x runs ---------------------------------

@@ -74,6 +74,21 @@ def test_wide_regions_bit_exact(params, oracle):
     _assert_same(b, ob, 4)
 
 
+def test_33_wide_regions_bit_exact(params, oracle):
+    """Unclipped 31-wide ROIs (33 x 33 regions) run on the narrow kernel with
+    the shifted mapping; a clipped one near the edge falls back to the wide
+    kernel; both match the oracle bit for bit."""
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, r, seed=40 + r) for r in (13, 14, 15)]
+    tumors.append(wl.disc_tumor(params, 14, seed=44, center=(15, 26)))
+    protocols = [[(0, 1.5), (700, 2.0)]]
+    st = np.array([0, 1, 2, 3, 1, 0], np.int32)
+    sp = np.zeros(6, np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 1100, seed=31)
+    assert (c == co).all()
+    _assert_same(b, ob, 6)
+
+
 def test_ragged_horizons_and_queue(params, oracle):
     from emt6ro import workloads as wl
     tumors = [wl.disc_tumor(params, r, seed=30 + r) for r in (2, 7, 18)]
@@ -88,6 +103,37 @@ def test_ragged_horizons_and_queue(params, oracle):
         _assert_same(b, ob, len(st))
         for i in range(len(st)):
             assert b.step(i) == min(1000, int(hz[i]))
+
+
+def test_graph_replay_and_queue_bit_exact(params, oracle):
+    """CUDA-graph replay of the launch sequence (schedule bit 1), with and
+    without the work queue, gives the oracle's states; a reset and rerun
+    replays a re-captured graph (new epoch)."""
+    from emt6ro import workloads as wl
+    from emt6ro.batch import Batch
+    tumors = [wl.disc_tumor(params, r, seed=60 + r) for r in (6, 11, 16)]
+    protocols = [[(0, 2.0)], [(300, 1.0), (600, 1.0)]]
+    st = np.array([0, 1, 2, 2, 1, 0], np.int32)
+    sp = np.array([0, 1, 0, 1, 0, 1], np.int32)
+    hz = np.array([900, 500, 900, 700, 300, 900], np.uint32)
+    for mode in (2, 3):
+        b = Batch(params, tumors, protocols, st, sp, sim_horizon=hz, seed=12)
+        b.set_schedule(mode, 256)
+        b.run(900)
+        ob = oracle.Batch(oracle.params_copy(params.native), 6, 12)
+        for i in range(6):
+            ob.set(i, tumors[st[i]].sites, b.doses[sp[i]], horizon=int(hz[i]))
+        ob.run(900, nthreads=6)
+        _assert_same(b, ob, 6)
+        b.reset()
+        b.set_doses(b.doses)
+        b.run(900)
+        ob2 = oracle.Batch(oracle.params_copy(params.native), 6, 12)
+        for i in range(6):
+            ob2.set(i, tumors[st[i]].sites, b.doses[sp[i]], horizon=int(hz[i]), epoch=1)
+        ob2.run(900, nthreads=6)
+        _assert_same(b, ob2, 6)
+        assert b.launches() > 0
 
 
 def test_reset_gives_fresh_epoch(params, oracle):

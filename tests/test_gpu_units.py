@@ -207,10 +207,17 @@ def test_diffusion_step_parity(case, params, oracle):
     f64 = np.ascontiguousarray(fld.reshape(-1).astype(np.float64))
     L.orc_diffuse_f64(f64, H, W, roi, mask, ctypes.byref(po_p))
     nrow, ncol = roi[2] + 2, roi[3] + 2
-    variants = [1] if (nrow > 32 or ncol > 31) else [0, 1]
-    for v in variants:
+    ran = []
+    for v in (0, 1):
         g = np.ascontiguousarray(fld.reshape(-1).copy())
-        N.check(N.lib().emt6_test_diffuse(ctypes.byref(p), N.ptr(g), H, W, N.ptr(roi), v, 0))
+        rc = N.lib().emt6_test_diffuse(ctypes.byref(p), N.ptr(g), H, W, N.ptr(roi), v, 0)
+        if v == 0 and rc == N.EMT6_ERR_LIMIT:
+            # the narrow path holds regions up to 32 x 31, and 33 x 33 ones
+            # whose first and last ring are fixed
+            assert nrow > 32 or ncol > 31
+            continue
+        N.check(rc)
+        ran.append(v)
         assert g.tobytes() == f32.tobytes(), f"variant {v} differs from the FP32 oracle"
         gf = g.reshape(3, H, W).astype(np.float64)
         rf = f64.reshape(3, H, W)
@@ -218,3 +225,7 @@ def test_diffusion_step_parity(case, params, oracle):
             eps = 1e-3 * float(ext[f])
             rel = np.abs(gf[f] - rf[f]) / np.maximum(np.abs(rf[f]), eps)
             assert rel.max() <= 1e-5, (v, f, rel.max())
+    if nrow <= 32 and ncol <= 31:
+        assert ran == [0, 1]
+    if radius in (13, 14):
+        assert 0 in ran  # 31-wide unclipped ROI: the shifted narrow mapping
