@@ -473,7 +473,7 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
   const int field = wid / NP, part = wid % NP;
   const int roff = NP == 2 ? m->roff : 0, coff = NP == 2 ? m->coff : 0;
   int RH = (nrow - roff + NP - 1) / NP;
-  RH = (RH + 1) & ~1;
+  if (NP != 2) RH = (RH + 1) & ~1;  // the two-warp path takes any row count
   float *f = fld + field * p.HW;
   float4 *x = xch + field * 2 * NP * (NP == 2 ? 1 : 2) * 32;
   const float ext = p.ext[field], ca = p.da[field], cb = p.db[field], cd = p.dd[field];
@@ -483,20 +483,30 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
 #define EMT6_CALL(R, WD)                                                                   \
   diffuse_part<NP, R, WD>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, \
                           nf, bar, roff, coff)
-#define EMT6_CASES(WD)                   \
-  switch (RH) {                          \
-    case 2: EMT6_CALL(2, WD); break;     \
-    case 4: EMT6_CALL(4, WD); break;     \
-    case 6: EMT6_CALL(6, WD); break;     \
-    case 8: EMT6_CALL(8, WD); break;     \
-    case 10: EMT6_CALL(10, WD); break;   \
-    case 12: EMT6_CALL(12, WD); break;   \
-    case 14: EMT6_CALL(14, WD); break;   \
-    default:                             \
-      if constexpr (NP == 2) {           \
-        if (RH == 16) EMT6_CALL(16, WD); \
-      }                                  \
-      break;                             \
+#define EMT6_CASES(WD)                                    \
+  switch (RH) {                                           \
+    case 2: EMT6_CALL(2, WD); break;                      \
+    case 4: EMT6_CALL(4, WD); break;                      \
+    case 6: EMT6_CALL(6, WD); break;                      \
+    case 8: EMT6_CALL(8, WD); break;                      \
+    case 10: EMT6_CALL(10, WD); break;                    \
+    case 12: EMT6_CALL(12, WD); break;                    \
+    case 14: EMT6_CALL(14, WD); break;                    \
+    default:                                              \
+      if constexpr (NP == 2 && !WD) {                     \
+        switch (RH) {                                     \
+          case 3: EMT6_CALL(3, false); break;             \
+          case 5: EMT6_CALL(5, false); break;             \
+          case 7: EMT6_CALL(7, false); break;             \
+          case 9: EMT6_CALL(9, false); break;             \
+          case 11: EMT6_CALL(11, false); break;           \
+          case 13: EMT6_CALL(13, false); break;           \
+          case 15: EMT6_CALL(15, false); break;           \
+          case 16: EMT6_CALL(16, false); break;           \
+          default: break;                                 \
+        }                                                 \
+      }                                                   \
+      break;                                              \
   }
   if (!WIDE_OK || ncol <= 31) {
     EMT6_CASES(false)
