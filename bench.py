@@ -20,7 +20,9 @@ interior sites / time.
   cpu_baseline   the oracle port of the reference CPU path on the host cores,
                  on a 64-simulation sample of the same workload
 
---impl reference times that CPU path alone (all host threads).
+--impl reference times that CPU path (all host threads) and, where its cubin
+was built, the reference's own CUDA kernels on the same 40,000 simulations
+("ref_cuda").
 Under torchrun (--gpus N) every rank runs its own 40,000-simulation shard
 (weak scaling); the time is the max over ranks.
 """
@@ -56,11 +58,11 @@ def shard_range(total: int, rank: int, world: int):
     return lo, lo + base + (1 if rank < extra else 0)
 
 
-def config1(n_reps: int = 20):
+def ga_batch(n_reps: int = 20):
     from emt6ro import workloads as wl
     params = wl.default_parameters()
-    tumors = wl.tumors_config1(params, 20)
-    protocols = wl.protocols_config1(100)
+    tumors = wl.ga_tumors(params, 20)
+    protocols = wl.ga_protocols(100)
     T, P = len(tumors), len(protocols)
     sim_tumor = np.repeat(np.tile(np.arange(T), P), n_reps).astype(np.int32)
     sim_protocol = np.repeat(np.arange(P), T * n_reps).astype(np.int32)
@@ -142,10 +144,54 @@ def cpu_sample(params, tumors, protocols, sim_tumor, sim_protocol, steps, warmup
     return rates, threads, n_sample
 
 
+def ref_cuda_sample(params, tumors, protocols, sim_tumor, sim_protocol, steps, warmup,
+                    sim_steps):
+    """The reference's own CUDA kernels (compiled from its sources for sm_103a,
+    oracle/_ref/emt6ro_ref_sm103a.cubin) on the whole 40,000-simulation batch,
+    launched in the order of its Simulation::step, timed with CUDA events on
+    its stream over the same bench-step window as this project's kernels.
+    Returns a dict, or None when the cubin is absent."""
+    from oracle import pyrefgpu
+    from emt6ro import workloads as wl
+    if not pyrefgpu.available():
+        return None
+    import torch
+    total = (warmup + steps) * sim_steps
+    if total > 8192:
+        return {"unavailable": f"{total} steps exceed the 8192 checked to stay inside the "
+                               "reference's fixed buffers for this workload"}
+    doses = wl.protocol_doses(protocols, 480)
+    ref = pyrefgpu.RefGpuSimulation(params, tumors, doses, sim_tumor, sim_protocol, seed=1)
+    stream = torch.cuda.ExternalStream(ref.stream)
+    for _ in range(warmup):
+        ref.run(sim_steps)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for k in range(steps):
+        ev[k][0].record(stream)
+        ref.run(sim_steps)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    counts = ref.counts()
+    ref.close()
+    n = len(sim_tumor)
+    return {"value": n * sim_steps * SITES / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms,
+            "steps": steps, "warmup": warmup, "mean_count": float(counts.mean()),
+            "kind": "reference CUDA kernels built from its sources (nvcc 13, sm_103a, -O3), "
+                    "host loop restating Simulation::step",
+            "sample": f"all {n} simulations, steps {warmup * sim_steps}-{total}"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    params, tumors, protocols, st, sp = config1()
+    params, tumors, protocols, st, sp = ga_batch()
+    ref_cuda = None
+    if not args.no_ref_cuda:
+        ref_cuda = ref_cuda_sample(params, tumors, protocols, st, sp, args.steps, args.warmup,
+                                   args.sim_steps)
     rates, threads, n = cpu_sample(params, tumors, protocols, st, sp, args.steps, args.warmup,
                                    args.sim_steps)
     v = statistics.median(rates)
@@ -164,7 +210,41 @@ def run_reference(args, rank, world):
                                    "reference CPU path, one simulation per thread"},
         "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if ref_cuda is not None:
+        line["ref_cuda"] = ref_cuda
     return line
+
+
+def _e2e(args, params, tumors, protocols, dev, seed, world, dist, bins):
+    """The same workload end to end through emt6ro.simulation.Experiment: per
+    bench step the doses of that hour uploaded (add_irradiations), run, and the
+    living counts read back (get_results).  Returns (value, h2d, d2h bytes)."""
+    import torch
+    from emt6ro import simulation as sim
+    B = 20 * len(tumors) * len(protocols)
+    exp = sim.Experiment(params, tumors, 20, len(protocols), gpu_id=dev, seed=seed)
+    for w in range(args.warmup):
+        exp.add_irradiations(_window(protocols, w, args.sim_steps))
+        exp.run(args.sim_steps)
+        exp.get_results()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        exp.add_irradiations(_window(protocols, args.warmup + k, args.sim_steps))
+        exp.run(args.sim_steps)
+        res = exp.get_results()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    value = world * B * args.sim_steps * SITES * args.steps / e2e_s
+    h2d = len(protocols) * bins * 4     # dose table upload per add_irradiations
+    d2h = int(res.size) * 4             # living counts per get_results
+    del exp
+    return value, h2d, d2h
 
 
 def run_ours(args, rank, world, dist):
@@ -177,7 +257,11 @@ def run_ours(args, rank, world, dist):
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    params, tumors, protocols, st, sp = config1()
+    params, tumors, protocols, st, sp = ga_batch()
+    if args.sims:
+        # a stratified subset of the batch (profiling captures of a small case)
+        keep = np.unique(np.linspace(0, len(st) - 1, args.sims).astype(np.int64))
+        st, sp = st[keep], sp[keep]
     B = len(st)
     seed = 0xE6E6 + rank
 
@@ -218,28 +302,8 @@ def run_ours(args, rank, world, dist):
     bins = (144_000 + 299) // 300
     e2e_value = None
     h2d = d2h = 0
-    exp = sim.Experiment(params, tumors, 20, len(protocols), gpu_id=dev, seed=seed)
-    for w in range(args.warmup):
-        exp.add_irradiations(_window(protocols, w, args.sim_steps))
-        exp.run(args.sim_steps)
-        exp.get_results()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        exp.add_irradiations(_window(protocols, args.warmup + k, args.sim_steps))
-        exp.run(args.sim_steps)
-        res = exp.get_results()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * B * args.sim_steps * SITES * args.steps / e2e_s
-    h2d = len(protocols) * bins * 4     # dose table upload per add_irradiations
-    d2h = int(res.size) * 4             # living counts per get_results
-    del exp
+    if not args.no_e2e and not args.sims:
+        e2e_value, h2d, d2h = _e2e(args, params, tumors, protocols, dev, seed, world, dist, bins)
 
     # ---- roofline of the dominant kernel -------------------------------------
     peak = ctypes.c_double()
@@ -288,7 +352,7 @@ def run_ours(args, rank, world, dist):
     }
 
 
-def run_config2(args):
+def run_ragged(args):
     """Ragged batch: 30,000 simulations, disc radius 2-20, 0-12 doses, horizons
     {72k, 144k, 288k} steps (5, 10, 20 days) mixed uniformly, scaled by
     --horizon-scale; launch schedule chosen by the autotuner; reports the
@@ -297,7 +361,7 @@ def run_config2(args):
     from emt6ro import workloads as wl, autotune
     from emt6ro.batch import Batch
     params = wl.default_parameters()
-    tumors, prots, st, sp, hz = wl.ragged_config2(params, 30_000)
+    tumors, prots, st, sp, hz = wl.ragged_batch(params, 30_000)
     hz = np.maximum((hz.astype(np.float64) * args.horizon_scale).astype(np.uint32), 1)
     t0 = time.perf_counter()
     mode, chunk, table = autotune.tune(params, tumors, prots, st, sp, hz, sample=2432,
@@ -360,13 +424,20 @@ def main():
     ap.add_argument("--sim-steps", type=int, default=600)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", type=int, choices=[1, 2], default=1,
-                    help="1: GA batch (default, the headline); 2: ragged batch")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end API timing")
+    ap.add_argument("--sims", type=int, default=0,
+                    help="time a stratified subset of this many simulations (small "
+                         "profiling case; implies --no-e2e)")
+    ap.add_argument("--no-ref-cuda", action="store_true",
+                    help="--impl reference: skip timing the reference's CUDA kernels")
+    ap.add_argument("--workload", choices=["ga", "ragged"], default="ga",
+                    help="ga: 40,000-simulation GA batch (default, the headline); "
+                         "ragged: 30,000 simulations with mixed sizes and horizons")
     ap.add_argument("--horizon-scale", type=float, default=1.0,
-                    help="config 2: multiply the 72k/144k/288k-step horizons")
+                    help="ragged: multiply the 72k/144k/288k-step horizons")
     args = ap.parse_args()
-    if args.config == 2:
-        print(json.dumps(run_config2(args)), flush=True)
+    if args.workload == "ragged":
+        print(json.dumps(run_ragged(args)), flush=True)
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -381,7 +452,7 @@ def main():
     else:
         line = run_ours(args, rank, world, dist)
         if rank == 0 and not args.no_cpu_baseline:
-            params, tumors, protocols, st, sp = config1()
+            params, tumors, protocols, st, sp = ga_batch()
             rates, threads, n = cpu_sample(params, tumors, protocols, st, sp, 2, 1,
                                            args.sim_steps)
             line["cpu_baseline"] = {

@@ -87,7 +87,7 @@ def disc_tumor(params: Parameters, radius: float, seed: int,
     return TumorState(g)
 
 
-def protocol_config0():
+def protocol_2x125gy():
     """2 x 1.25 Gy at hours 12 and 36."""
     return [(12 * HOUR_STEPS, 1.25), (36 * HOUR_STEPS, 1.25)]
 
@@ -104,13 +104,13 @@ def random_protocol(rng, k: int, total_gy: float = 10.0, quantum: float = 0.25,
     return [(int(s) * grid, float(n) * quantum) for s, n in zip(slots, parts)]
 
 
-def protocols_config1(n: int = 100, seed: int = 1000):
+def ga_protocols(n: int = 100, seed: int = 1000):
     """1-8 doses, 0.25-Gy quanta, 10 Gy total, on the 30-min grid in the first 48 h."""
     rng = np.random.default_rng(seed)
     return [random_protocol(rng, int(rng.integers(1, 9))) for _ in range(n)]
 
 
-def tumors_config1(params: Parameters, n: int = 20, seed0: int = 1):
+def ga_tumors(params: Parameters, n: int = 20, seed0: int = 1):
     """n tumours, disc radius uniform in 6..14, seeds seed0.."""
     out = []
     for i in range(n):
@@ -120,7 +120,7 @@ def tumors_config1(params: Parameters, n: int = 20, seed0: int = 1):
     return out
 
 
-def ragged_config2(params: Parameters, n_sims: int = 30000, seed: int = 2024,
+def ragged_batch(params: Parameters, n_sims: int = 30000, seed: int = 2024,
                    horizons=(72_000, 144_000, 288_000), n_tumors: int = 64):
     """Ragged batch: disc radius 2..20, 0-12 doses, horizons mixed uniformly.
     Returns (tumours, protocols, sim_tumor, sim_protocol, sim_horizon)."""

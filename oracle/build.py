@@ -5,8 +5,17 @@ build_ref()     compiles the reference's own host-side sources where they lie
                 (only when the reference checkout is present) together with
                 oracle/ref_shim.cc -> oracle/_ref/libemt6_ref.so.  It never
                 copies reference sources; outputs go to oracle/_ref/ only.
+build_ref_cubin()  compiles the reference's CUDA sources where they lie
+                (src/emt6ro/{simulation,diffusion,statistics,cell,common}/*.cu,
+                nvcc -dc, the reference's own CMake flags: C++14, relocatable
+                device code) and device-links them into one sm_103a cubin,
+                oracle/_ref/emt6ro_ref_sm103a.cubin (reference checkout only;
+                the cubin holds device code alone, so it is the same file for
+                any host architecture).
+build_ref_gpu_driver()  compiles oracle/ref_gpu_driver.cu, the host loop that
+                launches that cubin's kernels -> oracle/_build/libref_gpu.so.
 
-Both are plain gcc/g++ invocations (no cmake, no reference build system).
+All are plain gcc/g++/nvcc invocations (no cmake, no reference build system).
 Every float expression is compiled with -ffp-contract=off so the oracle
 evaluates exactly what its source says on x86-64 and aarch64 alike.
 """
@@ -25,6 +34,10 @@ CUDA_INC = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
 
 ORACLE_LIB = BUILD / "liborc.so"
 REF_LIB = REF_OUT / "libemt6_ref.so"
+REF_CUBIN = REF_OUT / "emt6ro_ref_sm103a.cubin"
+REF_GPU_LIB = BUILD / "libref_gpu.so"
+NVCC = str(Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "bin" / "nvcc")
+GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
 def _arch_flags() -> list[str]:
@@ -92,6 +105,49 @@ def build_ref(force: bool = False) -> Path | None:
     return REF_LIB
 
 
+def build_ref_cubin(force: bool = False) -> Path | None:
+    """Reference device code -> one linked sm_103a cubin; None when absent."""
+    if not reference_available():
+        return REF_CUBIN if REF_CUBIN.exists() else None
+    src = REFERENCE_ROOT / "src"
+    cu = [src / "emt6ro" / f for f in ("simulation/simulation.cu", "diffusion/diffusion.cu",
+                                      "statistics/statistics.cu", "common/random-engine.cu",
+                                      "cell/cell.cu", "common/instr.cu")]
+    if not (force or _stale(REF_CUBIN, cu)):
+        return REF_CUBIN
+    objdir = REF_OUT / "cu"
+    objdir.mkdir(parents=True, exist_ok=True)
+    inc = ["-I", str(src), "-I", str(REFERENCE_ROOT / "third-party" / "json")]
+    from concurrent.futures import ThreadPoolExecutor
+    objs = [objdir / (s.stem + ".o") for s in cu]
+    with ThreadPoolExecutor(len(cu)) as ex:
+        list(ex.map(lambda so: _run([NVCC, *GENCODE, "-dc", "-O3", "-DNDEBUG", "-std=c++14",
+                                     *inc, "-Xcompiler", "-fPIC", "-w", str(so[0]), "-o",
+                                     str(so[1])]), zip(cu, objs)))
+    tmp = REF_OUT / "emt6ro_ref_sm103a.tmp.cubin"
+    _run([NVCC, *GENCODE, "-dlink", "--cubin", "-o", str(tmp), *map(str, objs)])
+    os.replace(tmp, REF_CUBIN)
+    return REF_CUBIN
+
+
+def build_ref_gpu_driver(force: bool = False) -> Path:
+    """Host loop for the reference's kernels (driver API) -> oracle/_build/libref_gpu.so."""
+    BUILD.mkdir(exist_ok=True)
+    srcs = [HERE / "ref_gpu_driver.cu", HERE / "emt6_oracle.h"]
+    if force or _stale(REF_GPU_LIB, srcs):
+        cuda = Path(NVCC).parent.parent
+        stubs = [d for d in (cuda / "lib64" / "stubs", cuda / "targets" / "sbsa-linux" / "lib" / "stubs",
+                             cuda / "lib" / "stubs") if d.exists()]
+        tmp = REF_GPU_LIB.with_suffix(".so.tmp")
+        _run([NVCC, *GENCODE, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
+              "-I", str(HERE), str(HERE / "ref_gpu_driver.cu"), "-o", str(tmp),
+              *[f"-L{d}" for d in stubs], "-lcuda"])
+        os.replace(tmp, REF_GPU_LIB)
+    return REF_GPU_LIB
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
+    print(build_ref_cubin(force=True))
+    print(build_ref_gpu_driver(force=True))
