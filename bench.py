@@ -291,6 +291,7 @@ def run_ours(args, rank, world, dist):
     total_ms = sum(times)
     diffused = b.diffused() - d0
     launches = b.launches() - l0
+    mean_count = float(b.counts().mean())
     if dist:
         t = torch.tensor([total_ms], device=f"cuda:{dev}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -314,8 +315,10 @@ def run_ours(args, rank, world, dist):
     traffic = None
     if profiles.exists():
         try:
-            traffic = json.loads(profiles.read_text()).get("dram_bytes_per_launch")
-        except ValueError:
+            cap = json.loads(profiles.read_text())["captured"]
+            # per launch each simulation's state is read and written once
+            traffic = (cap["dram_read_bytes"] + cap["dram_write_bytes"]) / cap["simulations"] * B
+        except (ValueError, KeyError, ZeroDivisionError):
             traffic = None
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
             "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
@@ -349,6 +352,7 @@ def run_ours(args, rank, world, dist):
         "roofline": roof,
         "roofline_hbm": roof_hbm,
         "diffused_site_substeps_per_step": diffused // args.steps,
+        "mean_count": mean_count,
     }
 
 
