@@ -404,6 +404,140 @@ def run_ragged(args):
     }
 
 
+def _spearman(a, b):
+    ra = np.argsort(np.argsort(a)).astype(np.float64)
+    rb = np.argsort(np.argsort(b)).astype(np.float64)
+    return float(np.corrcoef(ra, rb)[0, 1])
+
+
+def run_surrogate(args):
+    """Surrogate training on simulator output and one surrogate-screened GA
+    generation.
+
+    1. Training data: --train-protocols GA protocols (1-8 doses, 10 Gy, 0.25-Gy
+       quanta, 30-min grid in the first 48 h) x the 20 GA tumours, each pair
+       the mean final living-cell count of --train-reps simulations of
+       --horizon steps (default 144,000 = 10 days).  10% of the protocols are
+       held out.
+    2. Training: Adam, batch 4096, on the GPU by the library's tcgen05 BF16
+       kernels; the training step is timed alone with CUDA events.
+    3. GA generation: --population protocols x 20 tumours scored by the
+       surrogate; the best --elite-frac re-simulated with --elite-sims
+       simulations each (20 tumours x runs).  Plain scoring would simulate
+       every protocol like an elite, so its rate is elites / simulation time.
+    """
+    import torch
+    from emt6ro import surrogate as S, workloads as wl
+    from emt6ro.batch import Batch
+    params = wl.default_parameters()
+    tumors = wl.ga_tumors(params, 20)
+    T = len(tumors)
+    horizon = args.horizon
+    clocks = ClockSampler(0)
+    clocks.start()
+    # 1. training data
+    P = args.train_protocols
+    protocols = wl.ga_protocols(P, seed=2024)
+    pp = np.repeat(np.arange(P), T)
+    pt = np.tile(np.arange(T), P)
+    t0 = time.perf_counter()
+    y = S.simulate_means(params, tumors, protocols, pp, pt, args.train_reps, horizon, seed=11)
+    data_s = time.perf_counter() - t0
+    x = S.features(protocols, tumors, pp, pt)
+    train = pp < int(0.9 * P)
+    # 2. training
+    net = S.Surrogate(max_batch=4096, seed=0)
+    t0 = time.perf_counter()
+    net.fit(x[train], y[train], epochs=args.epochs, lr=args.lr, batch=4096)
+    fit_s = time.perf_counter() - t0
+    pred_held = net.predict(x[~train])
+    err = pred_held - y[~train]
+    held = {"rmse_cells": float(np.sqrt(np.mean(err ** 2))),
+            "mean_rel_error": float(np.mean(np.abs(err) / np.maximum(y[~train], 1.0))),
+            "r2": float(1 - np.mean(err ** 2) / np.var(y[~train])),
+            "pairs": int((~train).sum())}
+    # training-step throughput on one resident batch (CUDA events on the
+    # surrogate's stream)
+    xs = net._norm_x(x[train][:4096] if train.sum() >= 4096 else np.resize(x[train], (4096, 100)))
+    ts = np.zeros(4096, np.float32)
+    stream = net._stream()
+    xd, td = net._to_dev(xs), net._to_dev(ts)
+    from emt6ro import _native as Nat
+    L = Nat.lib()
+    for _ in range(5):
+        Nat.check(L.emt6_mlp_train_step(net._h, xd.data_ptr(), td.data_ptr(), 4096, 0.0, None))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 50
+    e0.record(stream)
+    for _ in range(reps):
+        Nat.check(L.emt6_mlp_train_step(net._h, xd.data_ptr(), td.data_ptr(), 4096, 0.0, None))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    step_ms = e0.elapsed_time(e1) / reps
+    flop_row = 2 * (128 * 512 + 2 * 512 * 512 + 512) + 2 * (2 * 512 * 512) + \
+        2 * (512 * 128 + 2 * 512 * 512)
+    tflops = flop_row * 4096 / (step_ms * 1e-3) / 1e12
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+    # 3. screened GA generation
+    pop = wl.ga_protocols(args.population, seed=99)
+    keep = max(1, int(round(args.elite_frac * len(pop))))
+    runs = max(1, args.elite_sims // T)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    elite, pred = S.prescreen(net, pop, tumors, keep)
+    score_s = time.perf_counter() - t0
+    st = np.tile(np.repeat(np.arange(T, dtype=np.int32), runs), keep)
+    sp = np.repeat(np.arange(keep, dtype=np.int32), T * runs)
+    elite_prots = [pop[i] for i in elite]
+    t0 = time.perf_counter()
+    counts = np.zeros(len(st), np.float64)
+    chunk = 40_000 // (T * runs) * (T * runs)
+    for lo in range(0, len(st), chunk):
+        hi = min(len(st), lo + chunk)
+        b = Batch(params, tumors, elite_prots, st[lo:hi], sp[lo:hi], seed=31 + lo)
+        b.run(horizon)
+        counts[lo:hi] = b.counts()
+        del b
+    sim_s = time.perf_counter() - t0
+    clocks.stop()
+    sim_mean = counts.reshape(keep, T * runs).mean(1)
+    pe = pred[elite]
+    plain_rate = keep / sim_s
+    screened_rate = len(pop) / (score_s + sim_s)
+    return {
+        "metric": "GA protocols scored/s", "value": screened_rate,
+        "unit": "protocols/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+        "ms_per_step": (score_s + sim_s) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 (surrogate), f32 (simulation)",
+        "data": "synthetic (seeded GA tumours and protocols); surrogate trained on simulator "
+                "output only",
+        "config": {"workload": f"surrogate-screened GA generation: {len(pop)} protocols x {T} "
+                               f"tumours, top {keep} re-simulated with {T * runs} simulations "
+                               f"each, {horizon}-step horizon",
+                   "train_pairs": int(train.sum()), "train_reps": args.train_reps,
+                   "epochs": args.epochs, "batch": 4096},
+        "plain_protocols_per_s": plain_rate, "speedup_vs_plain": screened_rate / plain_rate,
+        "elites": {"spearman": _spearman(pe, sim_mean),
+                   "mean_rel_error": float(np.mean(np.abs(pe - sim_mean) / sim_mean)),
+                   "rel_error_of_mean": float(abs(pe.mean() - sim_mean.mean()) / sim_mean.mean()),
+                   "simulated_mean": float(sim_mean.mean()), "predicted_mean": float(pe.mean())},
+        "held_out": held,
+        "timings_s": {"training_data": data_s, "fit": fit_s, "surrogate_scoring": score_s,
+                      "elite_simulation": sim_s},
+        "train_step": {"ms": step_ms, "tflops": tflops,
+                       "roofline": {"bound": "tensor", "achieved": tflops, "peak": bf16_peak,
+                                    "unit": "TFLOP/s", "frac": tflops / bf16_peak,
+                                    "traffic": None,
+                                    "algorithmic": f"{flop_row} flop per row x 4096 rows "
+                                                   "(forward, input-gradient and weight-"
+                                                   "gradient GEMMs)"}},
+        "clocks": clocks.summary(),
+    }
+
+
 def _window(protocols, k, sim_steps):
     """The (step, dose) pairs of each protocol falling in bench step k."""
     lo, hi = k * sim_steps, (k + 1) * sim_steps
@@ -434,12 +568,25 @@ def main():
                          "profiling case; implies --no-e2e)")
     ap.add_argument("--no-ref-cuda", action="store_true",
                     help="--impl reference: skip timing the reference's CUDA kernels")
-    ap.add_argument("--workload", choices=["ga", "ragged"], default="ga",
+    ap.add_argument("--workload", choices=["ga", "ragged", "surrogate"], default="ga",
                     help="ga: 40,000-simulation GA batch (default, the headline); "
-                         "ragged: 30,000 simulations with mixed sizes and horizons")
+                         "ragged: 30,000 simulations with mixed sizes and horizons; "
+                         "surrogate: surrogate training + a screened GA generation")
+    ap.add_argument("--horizon", type=int, default=144_000,
+                    help="surrogate: simulated steps per simulation")
+    ap.add_argument("--train-protocols", type=int, default=400)
+    ap.add_argument("--train-reps", type=int, default=2)
+    ap.add_argument("--epochs", type=int, default=1500)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--population", type=int, default=10_000)
+    ap.add_argument("--elite-frac", type=float, default=0.05)
+    ap.add_argument("--elite-sims", type=int, default=100)
     ap.add_argument("--horizon-scale", type=float, default=1.0,
                     help="ragged: multiply the 72k/144k/288k-step horizons")
     args = ap.parse_args()
+    if args.workload == "surrogate":
+        print(json.dumps(run_surrogate(args)), flush=True)
+        return
     if args.workload == "ragged":
         print(json.dumps(run_ragged(args)), flush=True)
         return

@@ -2,8 +2,9 @@
 
     python emt6-ro_gb300/build_ext.py
 
-Two translation units (kernels, host engine + C ABI) compiled in parallel by
-nvcc for sm_103a only, then linked into emt6ro/_lib/libemt6ro_gb300.so next
+Four translation units (step kernels, host engine + C ABI, the
+allocation-free entry point, the surrogate MLP) compiled in parallel by nvcc
+for sm_103a only, then linked into emt6ro/_lib/libemt6ro_gb300.so next
 to the Python package that loads it.  --fmad=false and -ffp-contract=off make
 every floating-point expression round exactly as written.
 """
@@ -21,7 +22,7 @@ INCLUDE = HERE.parent / "include"
 OUT_DIR = HERE / "emt6ro" / "_lib"
 LIB = OUT_DIR / "libemt6ro_gb300.so"
 OBJ_DIR = HERE / "_build"
-SOURCES = ["emt6_kernels.cu", "emt6_host.cu", "emt6_noalloc.cu"]
+SOURCES = ["emt6_kernels.cu", "emt6_host.cu", "emt6_noalloc.cu", "surrogate.cu"]
 HEADERS = ["emt6_device.cuh", "emt6_kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -39,7 +40,8 @@ def stale() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = [CSRC / s for s in SOURCES + HEADERS] + [INCLUDE / "emt6ro_gb300.h", Path(__file__)]
+    deps = [CSRC / s for s in SOURCES + HEADERS] + [INCLUDE / "emt6ro_gb300.h",
+                                                     INCLUDE / "emt6ro_surrogate.h", Path(__file__)]
     return any(d.stat().st_mtime > t for d in deps)
 
 

@@ -1,4 +1,5 @@
-"""ctypes binding of libemt6ro_gb300.so (the C ABI in include/emt6ro_gb300.h).
+"""ctypes binding of libemt6ro_gb300.so (the C ABI in include/emt6ro_gb300.h and
+include/emt6ro_surrogate.h).
 
 The CUDA library is the only implementation: if it is missing (and cannot be
 built in place because nvcc is absent) importing this module raises.
@@ -113,6 +114,18 @@ _SIGNATURES = {
     "emt6_simulate_noalloc": (_c.c_int, [_P(Params), _VP, _c.c_int32, _c.c_int32, _VP, _VP,
                                          _c.c_int64, _VP, _c.c_uint32, _c.c_uint32, _c.c_uint32,
                                          _c.c_uint32, _c.c_uint64, _VP, _VP]),
+    # surrogate MLP (include/emt6ro_surrogate.h)
+    "emt6_mlp_create": (_c.c_int, [_c.c_int32, _c.c_uint64, _c.c_int32, _P(_VP)]),
+    "emt6_mlp_destroy": (None, [_VP]),
+    "emt6_mlp_stream": (_VP, [_VP]),
+    "emt6_mlp_set_params": (_c.c_int, [_VP, _P(_VP)]),
+    "emt6_mlp_get_params": (_c.c_int, [_VP, _P(_VP)]),
+    "emt6_mlp_predict": (_c.c_int, [_VP, _VP, _c.c_int32, _VP]),
+    "emt6_mlp_train_step": (_c.c_int, [_VP, _VP, _VP, _c.c_int32, _c.c_float,
+                                       _P(_c.c_float)]),
+    "emt6_mlp_gradients": (_c.c_int, [_VP, _VP, _VP, _c.c_int32, _P(_VP), _P(_c.c_float)]),
+    "emt6_mlp_sync": (_c.c_int, [_VP]),
+    "emt6_test_mlp_gemm": (_c.c_int, [_VP, _VP, _VP, _c.c_int32, _c.c_int32, _c.c_int32, _VP]),
 }
 
 _lib = None

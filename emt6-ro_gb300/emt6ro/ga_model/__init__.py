@@ -1,1 +1,2 @@
 from .model import EMT6RoModel
+from .screened import ScreenedModel
