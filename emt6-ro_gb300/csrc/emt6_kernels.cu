@@ -274,7 +274,10 @@ __device__ void narrow_mapping(const uint64_t *colmask, Misc *m) {
 // diffusion of one field by one warp of NP (part k = region rows
 // [k*RH, (k+1)*RH) of the (h+2) x (w+2) region; lane = column, or columns
 // 2*lane, 2*lane+1 when WIDE).
-// x' = a*x + b*(H + (x_up + x_down)) + d*(H_up + H_down), H = x_left + x_right.
+// With H = x_left + x_right and G = b*x + d*H per site (fmaf(d, H, b*x)):
+//   x' = a*x + b*(H + x_up + x_down) + d*(H_up + H_down)
+//      = fmaf(a, x, fmaf(b, H, G_up + G_down))
+// so a site needs its own x and H and the G of the rows above and below.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void named_barrier(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
@@ -296,19 +299,20 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
   const int j0 = (WIDE ? 2 * lane : lane) + coff;
   const int j1 = 2 * lane + 1;
   const int left = (lane + 31) & 31, right = (lane + 1) & 31;
-  const uint32_t rowsel = (1u << RH) - 1u;
+  const uint32_t rowsel = RH >= 32 ? 0xFFFFFFFFu : (1u << RH) - 1u;
   const uint32_t fm0 = (j0 < ncol) ? (uint32_t)(colmask[j0] >> base) & rowsel : 0u;
   const uint32_t fm1 = (WIDE && j1 < ncol) ? (uint32_t)(colmask[j1] >> base) & rowsel : 0u;
   const uint32_t roirows = (uint32_t)(((((1ull << h) - 1ull) << 1)) >> base) & rowsel;
   const uint32_t rm0 = (j0 >= 1 && j0 <= w) ? roirows : 0u;
   const uint32_t rm1 = (WIDE && j1 >= 1 && j1 <= w) ? roirows : 0u;
   const int lat0 = (r0 - 1) * W + (c0 - 1);
-  // the row above part 0: the zero ring, or region row 0 held at the external
-  // level when the mapping starts at row 1 (evaluated where used)
-  auto top_x = [&]() -> float { return (roff && j0 < ncol) ? ext : 0.f; };
-  auto top_h = [&]() -> float {
-    return roff ? ((j0 - 1 >= 0 && j0 - 1 < ncol) ? ext : 0.f) + ((j0 + 1 < ncol) ? ext : 0.f)
-                : 0.f;
+  // G of the row above part 0: the zero ring (G = 0), or region row 0 held at
+  // the external level when the mapping starts at row 1
+  auto top_g = [&]() -> float {
+    if (!roff) return 0.f;
+    const float tx = (j0 < ncol) ? ext : 0.f;
+    const float th = ((j0 - 1 >= 0 && j0 - 1 < ncol) ? ext : 0.f) + ((j0 + 1 < ncol) ? ext : 0.f);
+    return fmaf(cd, th, cb * tx);
   };
 
   float x0[RH], x1[WIDE ? RH : 1];
@@ -336,116 +340,125 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
 #pragma unroll
       for (int i = 0; i < RH; ++i)
         h0[i] = __shfl_sync(kFull, x0[i], left) + __shfl_sync(kFull, x0[i], right);
-      // Producer/consumer exchange with the partner warp: publish the boundary
-      // row, arrive on this part's barrier, update every row that does not
-      // need the partner, then wait on the partner's barrier for its row.
-      // Barrier ids alternate with the substep parity so a warp that runs a
-      // substep ahead never arrives twice on one barrier instance.
+      // Producer/consumer exchange with the partner warp: publish the
+      // boundary row's G, arrive on this part's barrier, update every row that
+      // does not need the partner, then wait on the partner's barrier for its
+      // G.  Barrier ids alternate with the substep parity so a warp that runs
+      // a substep ahead never arrives twice on one barrier instance.
       const int own = bar_id + par * 2 + part, other = bar_id + par * 2 + (1 - part);
       if (part == 0) {
-        *slot(par, 0, 1) = make_float4(x0[RH - 1], h0[RH - 1], 0.f, 0.f);
+        const float gl = fmaf(cd, h0[RH - 1], cb * x0[RH - 1]);
+        slot(par, 0, 1)->x = gl;
         named_arrive(own, 64);
-        float xm0 = top_x(), hm0 = top_h();
+        float gm = top_g();
+        float gc = RH > 1 ? fmaf(cd, h0[0], cb * x0[0]) : gl;
 #pragma unroll
         for (int i = 0; i < RH - 1; ++i) {
-          const float nv0 =
-              fmaf(ca, x0[i], fmaf(cb, h0[i] + (xm0 + x0[i + 1]), cd * (hm0 + h0[i + 1])));
-          xm0 = x0[i];
+          const float gn = (i + 1 == RH - 1) ? gl : fmaf(cd, h0[i + 1], cb * x0[i + 1]);
+          const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i], gm + gn));
           if ((u0 >> i) & 1u) x0[i] = nv0;
-          hm0 = h0[i];
+          gm = gc;
+          gc = gn;
         }
         named_barrier(other, 64);
-        const float4 nx = *slot(par, 1, 0);
-        const float nv0 =
-            fmaf(ca, x0[RH - 1], fmaf(cb, h0[RH - 1] + (xm0 + nx.x), cd * (hm0 + nx.y)));
+        const float gx = slot(par, 1, 0)->x;
+        const float nv0 = fmaf(ca, x0[RH - 1], fmaf(cb, h0[RH - 1], gm + gx));
         if ((u0 >> (RH - 1)) & 1u) x0[RH - 1] = nv0;
       } else {
-        *slot(par, 1, 0) = make_float4(x0[0], h0[0], 0.f, 0.f);
+        const float gf = fmaf(cd, h0[0], cb * x0[0]);
+        slot(par, 1, 0)->x = gf;
         named_arrive(own, 64);
-        const float x_first = x0[0], x_second = RH > 1 ? x0[1] : 0.f;
-        float xm0 = x0[0], hm0 = h0[0];
+        const float x_first = x0[0];
+        // G of row 1, taken before the loop overwrites x0[1]
+        const float g_second = RH > 1 ? fmaf(cd, h0[RH > 1 ? 1 : 0], cb * x0[RH > 1 ? 1 : 0]) : 0.f;
+        float gm = gf, gc = g_second;
 #pragma unroll
         for (int i = 1; i < RH; ++i) {
-          const float xn0 = (i + 1 < RH) ? x0[i + 1] : 0.f;
-          const float hn0 = (i + 1 < RH) ? h0[i + 1] : 0.f;
-          const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i] + (xm0 + xn0), cd * (hm0 + hn0)));
-          xm0 = x0[i];
+          const float gn = (i + 1 < RH) ? fmaf(cd, h0[i + 1], cb * x0[i + 1]) : 0.f;
+          const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i], gm + gn));
           if ((u0 >> i) & 1u) x0[i] = nv0;
-          hm0 = h0[i];
+          gm = gc;
+          gc = gn;
         }
         named_barrier(other, 64);
-        const float4 pv = *slot(par, 0, 1);
-        const float hn0 = RH > 1 ? h0[1] : 0.f;
-        const float nv0 =
-            fmaf(ca, x_first, fmaf(cb, h0[0] + (pv.x + x_second), cd * (pv.y + hn0)));
+        const float gp = slot(par, 0, 1)->x;
+        const float nv0 = fmaf(ca, x_first, fmaf(cb, h0[0], gp + g_second));
         if (u0 & 1u) x0[0] = nv0;
       }
     } else if constexpr (!WIDE) {
-      // RH = 16: horizontal sums on the fly (the two-phase form needs 16 more
+      // RH 15-16: horizontal sums on the fly (the two-phase form needs RH more
       // registers than the narrow kernel's budget)
       const float ht0 = __shfl_sync(kFull, x0[0], left) + __shfl_sync(kFull, x0[0], right);
       const float hb0 =
           __shfl_sync(kFull, x0[RH - 1], left) + __shfl_sync(kFull, x0[RH - 1], right);
-      if (part > 0) *slot(par, part, 0) = make_float4(x0[0], ht0, 0.f, 0.f);
-      if (part < NP - 1) *slot(par, part, 1) = make_float4(x0[RH - 1], hb0, 0.f, 0.f);
+      const float gt = fmaf(cd, ht0, cb * x0[0]);
+      const float gb = fmaf(cd, hb0, cb * x0[RH - 1]);
+      if (part > 0) slot(par, part, 0)->x = gt;
+      if (part < NP - 1) slot(par, part, 1)->x = gb;
       named_barrier(bar_id, NP * 32);
-      float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), nx = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (part > 0) pv = *slot(par, part - 1, 1);
-      else pv = make_float4(top_x(), top_h(), 0.f, 0.f);
-      if (part < NP - 1) nx = *slot(par, part + 1, 0);
-      float xm0 = pv.x, hm0 = pv.y, hc0 = ht0;
+      float gm = part > 0 ? slot(par, part - 1, 1)->x : top_g();
+      const float gx = part < NP - 1 ? slot(par, part + 1, 0)->x : 0.f;
+      float hc0 = ht0, gc = gt;
 #pragma unroll
       for (int i = 0; i < RH; ++i) {
-        float xn0, hn0;
+        float hn0 = 0.f, gn;
         if (i + 1 < RH) {
-          xn0 = x0[i + 1];
-          hn0 = __shfl_sync(kFull, xn0, left) + __shfl_sync(kFull, xn0, right);
+          const float xn0 = x0[i + 1];
+          hn0 = (i + 1 == RH - 1) ? hb0
+                                  : __shfl_sync(kFull, xn0, left) + __shfl_sync(kFull, xn0, right);
+          gn = (i + 1 == RH - 1) ? gb : fmaf(cd, hn0, cb * xn0);
         } else {
-          xn0 = nx.x;
-          hn0 = nx.y;
+          gn = gx;
         }
-        const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0 + (xm0 + xn0), cd * (hm0 + hn0)));
-        xm0 = x0[i];
+        const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0, gm + gn));
         if ((u0 >> i) & 1u) x0[i] = nv0;
-        hm0 = hc0;
+        gm = gc;
+        gc = gn;
         hc0 = hn0;
       }
     } else {
-      {
-        const float ht0 = __shfl_sync(kFull, x1[0], left) + x1[0];
-        const float ht1 = x0[0] + __shfl_sync(kFull, x0[0], right);
-        const float hb0 = __shfl_sync(kFull, x1[RH - 1], left) + x1[RH - 1];
-        const float hb1 = x0[RH - 1] + __shfl_sync(kFull, x0[RH - 1], right);
-        if (part > 0) *slot(par, part, 0) = make_float4(x0[0], ht0, x1[0], ht1);
-        if (part < NP - 1) *slot(par, part, 1) = make_float4(x0[RH - 1], hb0, x1[RH - 1], hb1);
-      }
+      const float ht0 = __shfl_sync(kFull, x1[0], left) + x1[0];
+      const float ht1 = x0[0] + __shfl_sync(kFull, x0[0], right);
+      const float hb0 = __shfl_sync(kFull, x1[RH - 1], left) + x1[RH - 1];
+      const float hb1 = x0[RH - 1] + __shfl_sync(kFull, x0[RH - 1], right);
+      const float gt0 = fmaf(cd, ht0, cb * x0[0]), gt1 = fmaf(cd, ht1, cb * x1[0]);
+      const float gb0 = fmaf(cd, hb0, cb * x0[RH - 1]), gb1 = fmaf(cd, hb1, cb * x1[RH - 1]);
+      if (part > 0) *slot(par, part, 0) = make_float4(gt0, gt1, 0.f, 0.f);
+      if (part < NP - 1) *slot(par, part, 1) = make_float4(gb0, gb1, 0.f, 0.f);
       named_barrier(bar_id, NP * 32);
       float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), nx = make_float4(0.f, 0.f, 0.f, 0.f);
       if (part > 0) pv = *slot(par, part - 1, 1);
       if (part < NP - 1) nx = *slot(par, part + 1, 0);
-      float xm0 = pv.x, hm0 = pv.y, xm1 = pv.z, hm1 = pv.w;
-      float hc0 = __shfl_sync(kFull, x1[0], left) + x1[0];
-      float hc1 = x0[0] + __shfl_sync(kFull, x0[0], right);
+      float gm0 = pv.x, gm1 = pv.y, gc0 = gt0, gc1 = gt1, hc0 = ht0, hc1 = ht1;
 #pragma unroll
       for (int i = 0; i < RH; ++i) {
-        float xn0, hn0, xn1, hn1;
+        float hn0 = 0.f, hn1 = 0.f, gn0, gn1;
         if (i + 1 < RH) {
-          xn0 = x0[i + 1];
-          xn1 = x1[i + 1];
-          hn0 = __shfl_sync(kFull, xn1, left) + xn1;
-          hn1 = xn0 + __shfl_sync(kFull, xn0, right);
+          const float xn0 = x0[i + 1], xn1 = x1[i + 1];
+          if (i + 1 == RH - 1) {
+            hn0 = hb0;
+            hn1 = hb1;
+            gn0 = gb0;
+            gn1 = gb1;
+          } else {
+            hn0 = __shfl_sync(kFull, xn1, left) + xn1;
+            hn1 = xn0 + __shfl_sync(kFull, xn0, right);
+            gn0 = fmaf(cd, hn0, cb * xn0);
+            gn1 = fmaf(cd, hn1, cb * xn1);
+          }
         } else {
-          xn0 = nx.x; hn0 = nx.y; xn1 = nx.z; hn1 = nx.w;
+          gn0 = nx.x;
+          gn1 = nx.y;
         }
-        const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0 + (xm0 + xn0), cd * (hm0 + hn0)));
-        const float nv1 = fmaf(ca, x1[i], fmaf(cb, hc1 + (xm1 + xn1), cd * (hm1 + hn1)));
-        xm0 = x0[i];
-        xm1 = x1[i];
+        const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0, gm0 + gn0));
+        const float nv1 = fmaf(ca, x1[i], fmaf(cb, hc1, gm1 + gn1));
         if ((u0 >> i) & 1u) x0[i] = nv0;
         if ((u1 >> i) & 1u) x1[i] = nv1;
-        hm0 = hc0;
+        gm0 = gc0;
+        gc0 = gn0;
+        gm1 = gc1;
+        gc1 = gn1;
         hc0 = hn0;
-        hm1 = hc1;
         hc1 = hn1;
       }
     }

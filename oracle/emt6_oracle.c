@@ -460,6 +460,7 @@ void orc_diffuse_f32(float *fld, int H, int W, const int32_t roi[5], const uint8
   float *X = (float *)calloc((size_t)tn, sizeof(float));
   float *Y = (float *)calloc((size_t)tn, sizeof(float));
   float *Hs = (float *)calloc((size_t)tn, sizeof(float));
+  float *G = (float *)calloc((size_t)tn, sizeof(float));
   int nfree = nsub - 1 > 0 ? nsub - 1 : 0;
   for (int f = 0; f < 3; ++f) {
     float *L = fld + (size_t)f * H * W;
@@ -470,24 +471,30 @@ void orc_diffuse_f32(float *fld, int H, int W, const int32_t roi[5], const uint8
         ORC_TILE(X, i, j) = mask[i * ncol + j] ? ext : L[(r0 - 1 + i) * W + (c0 - 1 + j)];
     for (int s = 0; s <= nfree; ++s) {
       int final = (s == nfree);
+      /* H = left + right, G = b*x + d*H (rounded as fmaf(d, H, b*x));
+       * x' = a*x + b*(H + up + down) + d*(H_up + H_down)
+       *    = fmaf(a, x, fmaf(b, H, G_up + G_down)) */
       for (int i = -1; i <= nrow; ++i)
-        for (int j = 0; j < ncol; ++j)
-          ORC_TILE(Hs, i, j) = ORC_TILE(X, i, j - 1) + ORC_TILE(X, i, j + 1);
+        for (int j = 0; j < ncol; ++j) {
+          const float hs = ORC_TILE(X, i, j - 1) + ORC_TILE(X, i, j + 1);
+          ORC_TILE(Hs, i, j) = hs;
+          ORC_TILE(G, i, j) = fmaf(d[f], hs, b[f] * ORC_TILE(X, i, j));
+        }
       memcpy(Y, X, sizeof(float) * tn);
       for (int i = 0; i < nrow; ++i)
         for (int j = 0; j < ncol; ++j) {
           int upd = final ? (i >= 1 && i <= h && j >= 1 && j <= w) : !mask[i * ncol + j];
           if (!upd) continue;
-          float orth = ORC_TILE(Hs, i, j) + (ORC_TILE(X, i - 1, j) + ORC_TILE(X, i + 1, j));
-          float diag = ORC_TILE(Hs, i - 1, j) + ORC_TILE(Hs, i + 1, j);
-          ORC_TILE(Y, i, j) = fmaf(a[f], ORC_TILE(X, i, j), fmaf(b[f], orth, d[f] * diag));
+          ORC_TILE(Y, i, j) = fmaf(a[f], ORC_TILE(X, i, j),
+                                   fmaf(b[f], ORC_TILE(Hs, i, j),
+                                        ORC_TILE(G, i - 1, j) + ORC_TILE(G, i + 1, j)));
         }
       float *tmp = X; X = Y; Y = tmp;
     }
     for (int i = 1; i <= h; ++i)
       for (int j = 1; j <= w; ++j) L[(r0 - 1 + i) * W + (c0 - 1 + j)] = ORC_TILE(X, i, j);
   }
-  free(X); free(Y); free(Hs);
+  free(X); free(Y); free(Hs); free(G);
 }
 
 /* The reference's own expression (diffusion.cu:122-133) in FP32, used by the
