@@ -189,11 +189,19 @@ class Surrogate:
 
     # ---- training / inference in living cells -------------------------------
     def fit(self, x, y, epochs: int = 60, lr: float = 1e-3, batch: int = 4096, seed: int = 0,
-            lr_final: float = 1e-5, verbose: bool = False):
+            lr_final: float = 1e-5, val_frac: float = 0.0, verbose: bool = False):
         """Adam on the MSE of standardised targets, cosine learning-rate decay
-        from lr to lr_final; drops the last partial batch of each epoch."""
+        from lr to lr_final; drops the last partial batch of each epoch.
+        With val_frac > 0 that share of the rows is held out and the
+        parameters of the epoch with the lowest validation error are kept."""
         x = np.asarray(x, np.float32)
         y = np.asarray(y, np.float64)
+        xv = yv = None
+        if val_frac > 0:
+            order = np.random.default_rng(seed + 1).permutation(len(x))
+            nv = max(1, int(round(val_frac * len(x))))
+            xv, yv = x[order[:nv]], y[order[:nv]]
+            x, y = x[order[nv:]], y[order[nv:]]
         if batch > self.max_batch or batch % 128:
             raise ValueError("batch must be a multiple of 128 up to max_batch")
         # a training set smaller than one batch trains on all of it each step
@@ -225,6 +233,8 @@ class Surrogate:
         loss = ctypes.c_float()
         k = 0
         t0 = time.perf_counter()
+        best, best_params = np.inf, None
+        self.val_history: list[float] = []
         for ep in range(epochs):
             perm = torch.from_numpy(rng.permutation(n)[: steps_per_epoch * batch]).to(xd.device)
             with torch.cuda.stream(self._stream()):
@@ -240,9 +250,16 @@ class Surrogate:
                     k += 1
                 ep_loss = loss.value
             self.history.append(ep_loss)
+            if xv is not None:
+                err = float(np.mean((self.predict(xv) - yv) ** 2))
+                self.val_history.append(err)
+                if err < best:
+                    best, best_params = err, self.get_params()
             if verbose:
                 print(f"epoch {ep}: loss {ep_loss:.4f} ({time.perf_counter() - t0:.1f}s)")
         N.check(N.lib().emt6_mlp_sync(self._h))
+        if best_params is not None:
+            self.set_params(best_params)
         return self.history
 
     def predict(self, x) -> np.ndarray:
