@@ -48,6 +48,10 @@ import numpy as np  # noqa: E402
 SITES = 51 * 51
 METRIC = "site-updates/s"
 FLOP_PER_SITE_SUBSTEP = 33  # 3 fields x 11 flop (9-point stencil + update)
+# surrogate training, per row: forward GEMMs 2(128*512 + 2*512*512 + 512),
+# input-gradient GEMMs 2(2*512*512), weight-gradient GEMMs 2(512*128 + 2*512*512)
+SURROGATE_FLOP_ROW = 2 * (128 * 512 + 2 * 512 * 512 + 512) + 2 * (2 * 512 * 512) + \
+    2 * (512 * 128 + 2 * 512 * 512)
 BYTES_PER_SITE_SUBSTEP = 24  # 3 fields x (4 B read + 4 B write)
 
 
@@ -454,7 +458,7 @@ def run_surrogate(args):
     pred_held = net.predict(x[~train])
     err = pred_held - y[~train]
     held = {"rmse_cells": float(np.sqrt(np.mean(err ** 2))),
-            "mean_rel_error": float(np.mean(np.abs(err) / np.maximum(y[~train], 1.0))),
+            "rmse_over_mean": float(np.sqrt(np.mean(err ** 2)) / np.mean(y[~train])),
             "r2": float(1 - np.mean(err ** 2) / np.var(y[~train])),
             "pairs": int((~train).sum())}
     # training-step throughput on one resident batch (CUDA events on the
@@ -476,12 +480,9 @@ def run_surrogate(args):
     e1.record(stream)
     torch.cuda.synchronize()
     step_ms = e0.elapsed_time(e1) / reps
-    flop_row = 2 * (128 * 512 + 2 * 512 * 512 + 512) + 2 * (2 * 512 * 512) + \
-        2 * (512 * 128 + 2 * 512 * 512)
+    flop_row = SURROGATE_FLOP_ROW
     tflops = flop_row * 4096 / (step_ms * 1e-3) / 1e12
-    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
-        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+    bf16_peak = _measured_bf16()
     # 3. screened GA generation
     pop = wl.ga_protocols(args.population, seed=99)
     keep = max(1, int(round(args.elite_frac * len(pop))))
@@ -540,6 +541,54 @@ def run_surrogate(args):
     }
 
 
+def run_surrogate_train(args):
+    """The surrogate's training step alone: Adam steps at batch 4096 on one
+    resident batch of standardised synthetic rows, timed with CUDA events on
+    the surrogate's stream; reports TFLOP/s against the measured BF16 peak."""
+    import torch
+    from emt6ro import _native as Nat
+    from emt6ro.surrogate import Surrogate, N_FEATURES
+    net = Surrogate(max_batch=4096, seed=0)
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=(4096, N_FEATURES)).astype(np.float32)
+    t = rng.normal(size=4096).astype(np.float32)
+    xd, td = net._to_dev(x), net._to_dev(t)
+    L = Nat.lib()
+    stream = net._stream()
+    for _ in range(args.warmup):
+        Nat.check(L.emt6_mlp_train_step(net._h, xd.data_ptr(), td.data_ptr(), 4096, 1e-4, None))
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        Nat.check(L.emt6_mlp_train_step(net._h, xd.data_ptr(), td.data_ptr(), 4096, 1e-4, None))
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    Nat.check(L.emt6_mlp_sync(net._h))
+    ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+    tflops = SURROGATE_FLOP_ROW * 4096 / (ms * 1e-3) / 1e12
+    peak = _measured_bf16()
+    return {"metric": "surrogate training steps/s", "value": 1e3 / ms, "unit": "steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "data": "synthetic standardised rows",
+            "config": {"workload": "surrogate MLP 100-512-512-512-1 training step, batch 4096"},
+            "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
+                         "frac": tflops / peak, "traffic": None,
+                         "algorithmic": f"{SURROGATE_FLOP_ROW} flop per row x 4096 rows"}}
+
+
+def _measured_bf16():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["bf16_tflops"])
+        except (ValueError, KeyError):
+            pass
+    return 1900.0
+
+
 def _window(protocols, k, sim_steps):
     """The (step, dose) pairs of each protocol falling in bench step k."""
     lo, hi = k * sim_steps, (k + 1) * sim_steps
@@ -570,7 +619,8 @@ def main():
                          "profiling case; implies --no-e2e)")
     ap.add_argument("--no-ref-cuda", action="store_true",
                     help="--impl reference: skip timing the reference's CUDA kernels")
-    ap.add_argument("--workload", choices=["ga", "ragged", "surrogate"], default="ga",
+    ap.add_argument("--workload", choices=["ga", "ragged", "surrogate", "surrogate-train"],
+                    default="ga",
                     help="ga: 40,000-simulation GA batch (default, the headline); "
                          "ragged: 30,000 simulations with mixed sizes and horizons; "
                          "surrogate: surrogate training + a screened GA generation")
@@ -586,6 +636,9 @@ def main():
     ap.add_argument("--horizon-scale", type=float, default=1.0,
                     help="ragged: multiply the 72k/144k/288k-step horizons")
     args = ap.parse_args()
+    if args.workload == "surrogate-train":
+        print(json.dumps(run_surrogate_train(args)), flush=True)
+        return
     if args.workload == "surrogate":
         print(json.dumps(run_surrogate(args)), flush=True)
         return

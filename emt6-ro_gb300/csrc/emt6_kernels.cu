@@ -325,9 +325,12 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
   }
 
   // exchange slot of (parity, part, side); side 0 = the part's first row
-  // (read by part - 1), side 1 = its last row (read by part + 1)
-  auto slot = [&](int par, int pt, int side) -> float4 * {
-    return xch + (NP == 2 ? (par * 2 + pt) : ((par * NP + pt) * 2 + side)) * 32 + lane;
+  // (read by part - 1), side 1 = its last row (read by part + 1).  One G per
+  // lane (two in the wide layout), packed so a warp's slot is 32 consecutive
+  // words (64-bit words when wide): conflict-free shared-memory accesses.
+  auto slot = [&](int par, int pt, int side) -> float * {
+    return reinterpret_cast<float *>(xch) +
+           ((NP == 2 ? (par * 2 + pt) : ((par * NP + pt) * 2 + side)) * 32 + lane) * (WIDE ? 2 : 1);
   };
   for (int s = 0; s <= nfree; ++s) {
     const bool fin = (s == nfree);
@@ -348,7 +351,7 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
       const int own = bar_id + par * 2 + part, other = bar_id + par * 2 + (1 - part);
       if (part == 0) {
         const float gl = fmaf(cd, h0[RH - 1], cb * x0[RH - 1]);
-        slot(par, 0, 1)->x = gl;
+        *slot(par, 0, 1) = gl;
         named_arrive(own, 64);
         float gm = top_g();
         float gc = RH > 1 ? fmaf(cd, h0[0], cb * x0[0]) : gl;
@@ -361,12 +364,12 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
           gc = gn;
         }
         named_barrier(other, 64);
-        const float gx = slot(par, 1, 0)->x;
+        const float gx = *slot(par, 1, 0);
         const float nv0 = fmaf(ca, x0[RH - 1], fmaf(cb, h0[RH - 1], gm + gx));
         if ((u0 >> (RH - 1)) & 1u) x0[RH - 1] = nv0;
       } else {
         const float gf = fmaf(cd, h0[0], cb * x0[0]);
-        slot(par, 1, 0)->x = gf;
+        *slot(par, 1, 0) = gf;
         named_arrive(own, 64);
         const float x_first = x0[0];
         // G of row 1, taken before the loop overwrites x0[1]
@@ -381,7 +384,7 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
           gc = gn;
         }
         named_barrier(other, 64);
-        const float gp = slot(par, 0, 1)->x;
+        const float gp = *slot(par, 0, 1);
         const float nv0 = fmaf(ca, x_first, fmaf(cb, h0[0], gp + g_second));
         if (u0 & 1u) x0[0] = nv0;
       }
@@ -393,11 +396,11 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
           __shfl_sync(kFull, x0[RH - 1], left) + __shfl_sync(kFull, x0[RH - 1], right);
       const float gt = fmaf(cd, ht0, cb * x0[0]);
       const float gb = fmaf(cd, hb0, cb * x0[RH - 1]);
-      if (part > 0) slot(par, part, 0)->x = gt;
-      if (part < NP - 1) slot(par, part, 1)->x = gb;
+      if (part > 0) *slot(par, part, 0) = gt;
+      if (part < NP - 1) *slot(par, part, 1) = gb;
       named_barrier(bar_id, NP * 32);
-      float gm = part > 0 ? slot(par, part - 1, 1)->x : top_g();
-      const float gx = part < NP - 1 ? slot(par, part + 1, 0)->x : 0.f;
+      float gm = part > 0 ? *slot(par, part - 1, 1) : top_g();
+      const float gx = part < NP - 1 ? *slot(par, part + 1, 0) : 0.f;
       float hc0 = ht0, gc = gt;
 #pragma unroll
       for (int i = 0; i < RH; ++i) {
@@ -423,12 +426,12 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
       const float hb1 = x0[RH - 1] + __shfl_sync(kFull, x0[RH - 1], right);
       const float gt0 = fmaf(cd, ht0, cb * x0[0]), gt1 = fmaf(cd, ht1, cb * x1[0]);
       const float gb0 = fmaf(cd, hb0, cb * x0[RH - 1]), gb1 = fmaf(cd, hb1, cb * x1[RH - 1]);
-      if (part > 0) *slot(par, part, 0) = make_float4(gt0, gt1, 0.f, 0.f);
-      if (part < NP - 1) *slot(par, part, 1) = make_float4(gb0, gb1, 0.f, 0.f);
+      if (part > 0) *reinterpret_cast<float2 *>(slot(par, part, 0)) = make_float2(gt0, gt1);
+      if (part < NP - 1) *reinterpret_cast<float2 *>(slot(par, part, 1)) = make_float2(gb0, gb1);
       named_barrier(bar_id, NP * 32);
-      float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), nx = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (part > 0) pv = *slot(par, part - 1, 1);
-      if (part < NP - 1) nx = *slot(par, part + 1, 0);
+      float2 pv = make_float2(0.f, 0.f), nx = make_float2(0.f, 0.f);
+      if (part > 0) pv = *reinterpret_cast<const float2 *>(slot(par, part - 1, 1));
+      if (part < NP - 1) nx = *reinterpret_cast<const float2 *>(slot(par, part + 1, 0));
       float gm0 = pv.x, gm1 = pv.y, gc0 = gt0, gc1 = gt1, hc0 = ht0, hc1 = ht1;
 #pragma unroll
       for (int i = 0; i < RH; ++i) {
@@ -535,10 +538,9 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
 // Site::step (site/site.h:62-82) on the CTA's lattice; returns ready-to-divide.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool step_site(const KParams &p, float *fld, uint8_t *st,
-                                          float4 *cells, int s, uint32_t vac, float dose,
-                                          uint32_t t, uint32_t sim, uint32_t occ,
+                                          float4 *cells, int s, DCell c, uint32_t vac,
+                                          float dose, uint32_t t, uint32_t sim, uint32_t occ,
                                           uint32_t epoch, Misc *m) {
-  DCell c = load_cell(cells + 3 * s);
   const int HW = p.HW;
   float l0 = fld[s], l1 = fld[HW + s], l2 = fld[2 * HW + s];
   if (!update_state(c, l0, l1, l2, p, vac)) {
@@ -720,18 +722,36 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
       bool any_ready = false;
       const float dose =
           (t < p.length && t % p.res == 0 && t / p.res < p.bins) ? doses[t / p.res] : 0.f;
-      for (uint32_t e = tid; e < n; e += NT) {
-        const int s = list[e];
-        const uint8_t sv = st[s];
-        if ((sv & kStMask) != kOccupied) {
-          if (!(sv & kStMulti)) aux[e] = 0;
-          continue;
+      {
+        // Software pipeline over this thread's entries: the next entry's cell
+        // record is loaded from L2 before the current entry is stepped.  Entries
+        // of sites listed once name distinct sites, so stepping the current
+        // entry never writes the record or state the early load reads.
+        uint32_t e = tid;
+        DCell nc{};
+        if (e < n) {
+          const int s0 = list[e];
+          if ((st[s0] & (kStMask | kStMulti)) == kOccupied) nc = load_cell(cells + 3 * s0);
         }
-        if (sv & kStMulti) continue;  // stepped in list order below
-        const bool ready = step_site(p, fld, st, cells, s, aux[e], dose, t, (uint32_t)sim, 0,
-                                     a.epoch, m);
-        aux[e] = ready ? 0x80 : 0;
-        any_ready |= ready;
+        for (; e < n; e += NT) {
+          const DCell c = nc;
+          const uint32_t en = e + NT;
+          if (en < n) {
+            const int s2 = list[en];
+            if ((st[s2] & (kStMask | kStMulti)) == kOccupied) nc = load_cell(cells + 3 * s2);
+          }
+          const int s = list[e];
+          const uint8_t sv = st[s];
+          if ((sv & kStMask) != kOccupied) {
+            if (!(sv & kStMulti)) aux[e] = 0;
+            continue;
+          }
+          if (sv & kStMulti) continue;  // stepped in list order below
+          const bool ready = step_site(p, fld, st, cells, s, c, aux[e], dose, t, (uint32_t)sim,
+                                       0, a.epoch, m);
+          aux[e] = ready ? 0x80 : 0;
+          any_ready |= ready;
+        }
       }
       if (m->has_multi && wid == 0) {
         // sites listed more than once: every entry steps the site, in list order
@@ -749,8 +769,9 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
               const int s = list[ee];
               uint8_t res = 0;
               if ((st[s] & kStMask) == kOccupied) {
-                const bool ready = step_site(p, fld, st, cells, s, aux[ee] & 15u, dose, t,
-                                             (uint32_t)sim, occ, a.epoch, m);
+                const bool ready = step_site(p, fld, st, cells, s, load_cell(cells + 3 * s),
+                                             aux[ee] & 15u, dose, t, (uint32_t)sim, occ,
+                                             a.epoch, m);
                 if (ready) {
                   if (occ > 127) atomicOr(a.err, 4u);
                   res = (uint8_t)(0x80 | (occ & 0x7f));
@@ -772,6 +793,17 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
         const uint8_t av = aux[e];
         if (av & 0x80) {
           const int s = list[e];
+          // a cell none of whose neighbours is vacant now cannot divide,
+          // whatever the draw: skip the draw (interior cells stay ready)
+          const bool open = ((st[s - W - 1] & kStMask) == kVacant) |
+                            ((st[s - W] & kStMask) == kVacant) |
+                            ((st[s - W + 1] & kStMask) == kVacant) |
+                            ((st[s - 1] & kStMask) == kVacant) |
+                            ((st[s + 1] & kStMask) == kVacant) |
+                            ((st[s + W - 1] & kStMask) == kVacant) |
+                            ((st[s + W] & kStMask) == kVacant) |
+                            ((st[s + W + 1] & kStMask) == kVacant);
+          if (!open) continue;
           const float u = u01(draw(p, t, (uint32_t)sim, (uint32_t)s, av & 0x7fu, 0, a.epoch).x);
           const int tg = choose_neighbour(s, W, u);
           if ((st[tg] & kStMask) == kVacant) {

@@ -256,11 +256,13 @@ __device__ __forceinline__ void epilogue(const EpiArgs &ep, int row, int col0, c
   }
 }
 
-// C tile (blockIdx.y, blockIdx.x) of C[M,N] = A[M,K] B[N,K]^T.
+// C tile (blockIdx.y, blockIdx.x) of C[M,N] = A[M,K] B[N,K]^T over the
+// k-blocks [blockIdx.z * nk, (blockIdx.z + 1) * nk) (split K: each z writes
+// its own FP32 partial tile, EPI_STORE_F32 only).
 template <int EPI>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     mlp_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                    int K, EpiArgs ep) {
+                    int nk, EpiArgs ep) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~static_cast<uintptr_t>(1023));
@@ -273,7 +275,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                  done = smem_u32(bars + 2 * STAGES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int nk = K / BK;
+  const int kb0 = blockIdx.z * nk;
+  if (EPI == EPI_STORE_F32 && blockIdx.z) ep.c_out += static_cast<size_t>(blockIdx.z) * ep.M * ep.N;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -303,8 +306,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         break;
       }
       mbar_expect_tx(full0 + 8 * s, 2 * TILE_BYTES);
-      tma_load_2d(smem_u32(sA + s * TILE_BYTES), &tmA, full0 + 8 * s, kb * BK, m0);
-      tma_load_2d(smem_u32(sB + s * TILE_BYTES), &tmB, full0 + 8 * s, kb * BK, n0);
+      tma_load_2d(smem_u32(sA + s * TILE_BYTES), &tmA, full0 + 8 * s, (kb0 + kb) * BK, m0);
+      tma_load_2d(smem_u32(sB + s * TILE_BYTES), &tmB, full0 + 8 * s, (kb0 + kb) * BK, n0);
       ++issued;
     }
     if (failed) {
@@ -525,7 +528,7 @@ bool make_map(CUtensorMap *map, const void *base, int rows, int cols) {
 
 template <int EPI>
 cudaError_t launch_gemm(const CUtensorMap &a, const CUtensorMap &b, int M, int N, int K,
-                        const EpiArgs &ep, cudaStream_t st) {
+                        const EpiArgs &ep, cudaStream_t st, int splits = 1) {
   static bool attr_set[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -536,9 +539,52 @@ cudaError_t launch_gemm(const CUtensorMap &a, const CUtensorMap &b, int M, int N
     if (e != cudaSuccess) return e;
     attr_set[dev] = true;
   }
-  dim3 grid(N / BN, M / BM);
-  mlp_gemm_kernel<EPI><<<grid, GEMM_THREADS, GEMM_SMEM, st>>>(a, b, K, ep);
+  dim3 grid(N / BN, M / BM, splits);
+  mlp_gemm_kernel<EPI><<<grid, GEMM_THREADS, GEMM_SMEM, st>>>(a, b, K / BK / splits, ep);
   return cudaGetLastError();
+}
+
+// Sum of the split-K partial tiles of a weight gradient g[M][N] in a fixed
+// order, then either the Adam update (FP32 master, moments, BF16 W and W^T)
+// or, with grad_out, the gradient itself.  32 x 32 tiles, 256 threads; W^T
+// goes through shared memory so both stores are coalesced.
+__global__ void __launch_bounds__(256) adam_reduce_kernel(const float *__restrict__ part, int splits,
+                                                          int M, int N, float *w, float *m,
+                                                          float *v, __nv_bfloat16 *w_bf,
+                                                          __nv_bfloat16 *w_bf_t, float *grad_out,
+                                                          float lr, float beta1, float beta2,
+                                                          float eps, float bc1, float bc2) {
+  __shared__ __nv_bfloat16 tile[32][34];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const size_t MN = static_cast<size_t>(M) * N;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = r0 + ty + 8 * i, c = c0 + tx;
+    const size_t k = static_cast<size_t>(r) * N + c;
+    float g = part[k];
+    for (int z = 1; z < splits; ++z) g += part[z * MN + k];
+    if (grad_out) {
+      grad_out[k] = g;
+      continue;
+    }
+    const float mm = beta1 * m[k] + (1.0f - beta1) * g;
+    const float vv = beta2 * v[k] + (1.0f - beta2) * g * g;
+    const float ww = w[k] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+    m[k] = mm;
+    v[k] = vv;
+    w[k] = ww;
+    const __nv_bfloat16 wb = __float2bfloat16_rn(ww);
+    w_bf[k] = wb;
+    tile[tx][ty + 8 * i] = wb;
+  }
+  if (grad_out) return;
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int c = c0 + ty + 8 * i, r = r0 + tx;
+    w_bf_t[static_cast<size_t>(c) * M + r] = tile[ty + 8 * i][tx];
+  }
 }
 
 template <typename T>
@@ -568,7 +614,8 @@ struct emt6_mlp {
   DevArr<__nv_bfloat16> wb[3], wbt[3];
   // activations for max_batch rows
   DevArr<__nv_bfloat16> X, XT, Z[3], A[3], AT[3], dZ[3], dZT[3];
-  DevArr<float> y, dy, loss, gradw[3], gradv[5];
+  DevArr<float> y, dy, loss, gradw[3], gradv[5], work;
+  int split_override = 0;  // 0: choose per batch size
   DevArr<int> err;
   CUtensorMap mX, mXT, mA[3], mAT[3], mW[3], mWT[3], mdZ[3], mdZT[3];
 };
@@ -639,6 +686,16 @@ bool build_maps(emt6_mlp *net, int B) {
   return ok;
 }
 
+// Split of the weight-gradient GEMMs' K (= B) dimension: the most of 8, 4, 2
+// that leaves every CTA at least 4 k-blocks of 64 rows.
+int weight_splits(const emt6_mlp *net, int B) {
+  const int nkb = B / BK;
+  if (net->split_override > 0) return nkb % net->split_override == 0 ? net->split_override : 1;
+  for (int sp : {8, 4, 2})
+    if (nkb % sp == 0 && nkb / sp >= 4) return sp;
+  return 1;
+}
+
 int backward(emt6_mlp *net, int B, const float *d_target, bool apply, float lr) {
   cudaStream_t st = net->stream;
   cudaError_t e;
@@ -664,7 +721,21 @@ int backward(emt6_mlp *net, int B, const float *d_target, bool apply, float lr) 
     }
     const CUtensorMap &bmap = l == 0 ? net->mXT : net->mAT[l - 1];
     const int N = cols_of(l);
-    if (apply) {
+    const int splits = weight_splits(net, B);
+    if (splits > 1) {
+      // K = B is long and M x N small: split K over `splits` CTAs per tile,
+      // then reduce the partial tiles in a fixed order (deterministic)
+      EpiArgs ep = base_args(net, net->H, N);
+      ep.c_out = net->work.p;
+      e = launch_gemm<EPI_STORE_F32>(net->mdZT[l], bmap, net->H, N, B, ep, st, splits);
+      if (e == cudaSuccess) {
+        adam_reduce_kernel<<<dim3(N / 32, net->H / 32), 256, 0, st>>>(
+            net->work.p, splits, net->H, N, net->w[l].p, net->m[l].p, net->v[l].p, net->wb[l].p,
+            net->wbt[l].p, apply ? nullptr : net->gradw[l].p, lr, net->beta1, net->beta2,
+            net->eps, bc1, bc2);
+        e = cudaGetLastError();
+      }
+    } else if (apply) {
       EpiArgs ep = base_args(net, net->H, N);
       ep.w = net->w[l].p;
       ep.m = net->m[l].p;
@@ -759,6 +830,7 @@ int emt6_mlp_create(int max_batch, uint64_t seed, int device, emt6_mlp **out) {
     ok = net->Z[l].alloc(BH) && net->A[l].alloc(BH) && net->AT[l].alloc(BH) &&
          net->dZ[l].alloc(BH) && net->dZT[l].alloc(BH);
   for (int i = 0; i < 5 && ok; ++i) ok = net->gradv[i].alloc(i < 4 ? H : 1);
+  ok = ok && net->work.alloc(static_cast<size_t>(8) * H * H);
   if (!ok) {
     if (net->stream) cudaStreamDestroy(net->stream);
     delete net;
@@ -908,6 +980,14 @@ int emt6_mlp_gradients(emt6_mlp *net, const float *d_x, const float *d_target, i
     *h_loss = s / static_cast<float>(B);
   }
   return e == cudaSuccess ? EMT6_OK : cuda_fail(e, "emt6_mlp_gradients");
+}
+
+int emt6_mlp_set_splitk(emt6_mlp *net, int splits) {
+  if (!net || (splits != 0 && splits != 1 && splits != 2 && splits != 4 && splits != 8))
+    return fail("emt6_mlp_set_splitk: splits must be 0 (automatic), 1, 2, 4 or 8",
+                EMT6_ERR_INVALID);
+  net->split_override = splits;
+  return EMT6_OK;
 }
 
 int emt6_mlp_sync(emt6_mlp *net) {

@@ -125,6 +125,7 @@ _SIGNATURES = {
                                        _P(_c.c_float)]),
     "emt6_mlp_gradients": (_c.c_int, [_VP, _VP, _VP, _c.c_int32, _P(_VP), _P(_c.c_float)]),
     "emt6_mlp_sync": (_c.c_int, [_VP]),
+    "emt6_mlp_set_splitk": (_c.c_int, [_VP, _c.c_int32]),
     "emt6_test_mlp_gemm": (_c.c_int, [_VP, _VP, _VP, _c.c_int32, _c.c_int32, _c.c_int32, _VP]),
 }
 

@@ -63,6 +63,11 @@ int emt6_mlp_train_step(emt6_mlp *net, const float *d_x, const float *d_target, 
 int emt6_mlp_gradients(emt6_mlp *net, const float *d_x, const float *d_target, int B,
                        float *const *host_grads, float *h_loss);
 
+/* Split of the weight-gradient GEMMs' reduction (batch) dimension over CTAs:
+ * 0 chooses per batch size (default), or 1, 2, 4, 8.  Partial tiles are summed
+ * in a fixed order, so results are deterministic for a given split. */
+int emt6_mlp_set_splitk(emt6_mlp *net, int splits);
+
 /* Waits for the handle's stream; EMT6_ERR_DEVICE if a GEMM's pipeline wait
  * timed out since the last check. */
 int emt6_mlp_sync(emt6_mlp *net);

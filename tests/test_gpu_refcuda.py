@@ -75,3 +75,37 @@ def test_distribution_matches_reference_cuda_build(name, params):
     fixture = GOLDEN / "dist_refcpu.npz"
     if fixture.exists():
         _close(np.load(fixture)[name].astype(np.float64), ref_counts)
+
+
+@pytest.mark.gpu
+def test_per_protocol_means_match_reference_cuda_build(params):
+    """The reference's validation notebook compares per-protocol means of two
+    simulators with Welch t-tests (simulation_analysis/results-comparison.ipynb,
+    cells 9-11).  Here: 20 random 10-Gy protocols x 100 replicates of the
+    radius-10 tumour over 36 h, this project's kernels against the reference's
+    CUDA build: per-protocol means within 6%, and no more than 2 of 20 Welch
+    tests below p = 0.01."""
+    from scipy import stats
+    from oracle import pyrefgpu
+    if not pyrefgpu.available():
+        pytest.skip("reference cubin not built (needs the reference checkout)")
+    import emt6ro.simulation as sim
+    from emt6ro import workloads as wl
+    tumor = wl.disc_tumor(params, 10, seed=0)
+    protocols = wl.ga_protocols(20, seed=606)
+    reps, steps = 100, 36 * 600
+    doses = wl.protocol_doses(protocols, 480)
+    sp = np.repeat(np.arange(20, dtype=np.int32), reps)
+    ref = pyrefgpu.RefGpuSimulation(params, [tumor], doses, np.zeros(len(sp), np.int32), sp,
+                                    seed=777)
+    ref.run(steps)
+    theirs = ref.counts().astype(np.float64).reshape(20, reps)
+    ref.close()
+    e = sim.Experiment(params, [tumor], reps, 20, seed=31)
+    e.add_irradiations(protocols)
+    e.run(steps)
+    ours = e.get_results().astype(np.float64).reshape(20, reps)
+    rel = np.abs(ours.mean(1) - theirs.mean(1)) / theirs.mean(1)
+    assert rel.max() < 0.06, rel
+    p = np.array([stats.ttest_ind(a, b, equal_var=False).pvalue for a, b in zip(ours, theirs)])
+    assert (p < 0.01).sum() <= 2, p

@@ -90,6 +90,36 @@ def test_gradients_match_oracle():
     assert np.all(g[0][:, 100:] == 0)          # padded inputs get no gradient
 
 
+def test_split_k_weight_gradients_agree():
+    """The weight-gradient GEMMs with the batch dimension split over 2, 4 or 8
+    CTAs (partial tiles reduced in a fixed order) agree with the unsplit
+    kernel, and one Adam step through the split path (reduce kernel) agrees
+    with the fused Adam epilogue."""
+    from emt6ro import _native as Nat
+    from oracle import mlp_oracle as mo
+    net, params = _net(7)
+    rng = np.random.default_rng(8)
+    x = rng.normal(size=(1024, 100)).astype(np.float32)
+    t = rng.normal(size=1024).astype(np.float32)
+    grads = {}
+    for sp in (1, 2, 4, 0):
+        Nat.check(Nat.lib().emt6_mlp_set_splitk(net._h, sp))
+        grads[sp], _ = net.gradients(x, t)
+    for sp in (2, 4, 0):
+        for a, b in zip(grads[sp], grads[1]):
+            assert _rel(a, b) < 1e-5
+    stepped = {}
+    for sp in (1, 4):
+        fresh, _ = _net(7)          # fresh Adam state
+        Nat.check(Nat.lib().emt6_mlp_set_splitk(fresh._h, sp))
+        fresh.train_step(x, t, 1e-3)
+        stepped[sp] = fresh.get_params()
+    for a, b in zip(stepped[1], stepped[4]):
+        assert np.mean(np.isclose(a, b, rtol=1e-4, atol=1e-6)) > 0.995
+    with pytest.raises(Nat.NativeError, match="splits"):
+        Nat.check(Nat.lib().emt6_mlp_set_splitk(net._h, 3))
+
+
 def test_adam_step_matches_oracle():
     from oracle import mlp_oracle as mo
     net, params = _net(5)
@@ -177,3 +207,27 @@ def test_validation_keeps_best_epoch(dataset_48h):
     nv = 256
     xv, yv = x[:1280][order[:nv]], y[:1280][order[:nv]]
     assert np.mean((net.predict(xv) - yv) ** 2) == pytest.approx(xv_err, rel=1e-5)
+
+
+def test_screened_model_simulates_only_the_elites(params, trained):
+    """ScreenedModel.predict: the drop-in for EMT6RoModel.predict that scores
+    every protocol with the surrogate and simulates only the best fraction;
+    elites carry their simulated fitness, the rest the predicted one."""
+    from emt6ro import workloads as wl
+    from emt6ro.ga_model import ScreenedModel, EMT6RoModel
+    tumors = wl.ga_tumors(params, 20)[:2]
+    protocols = wl.ga_protocols(12, seed=5)
+    model = ScreenedModel(params, tumors, trained, num_tests=2, keep_frac=0.25, num_steps=28_800,
+                          seed=3)
+    fit = model.predict(protocols)
+    assert fit.shape == (12,)
+    elite = model.last["elite"]
+    assert len(elite) == 3
+    assert np.allclose(fit[elite], 1500 - model.last["simulated"])
+    rest = np.setdiff1d(np.arange(12), elite)
+    from emt6ro.surrogate import prescreen
+    _, pred = prescreen(trained, protocols, tumors, 3)
+    assert np.allclose(fit[rest], 1500 - pred[rest])
+    # the elites' simulated fitness is what the plain model gives them
+    plain = EMT6RoModel(params, tumors, 3, 2, num_steps=28_800, seed=3)
+    assert np.allclose(plain.predict([protocols[i] for i in elite]), fit[elite])
