@@ -1,14 +1,14 @@
 // surrogate.cu -- the protocol-outcome surrogate: a 100 -> 512 -> 512 -> 512 -> 1
 // GELU MLP trained and evaluated on the GPU with hand-written kernels.
 //
-// GEMMs run on the 5th-generation tensor cores: one CTA of 128 threads owns a
+// GEMMs run on the 5th-generation tensor cores: one CTA of 512 threads owns a
 // 128 x 128 FP32 accumulator in tensor memory (TMEM, 128 columns); thread 0
 // streams 128 x 64 BF16 tiles of both operands into a 4-stage shared-memory
 // ring with TMA (128-byte swizzle), thread 32 issues tcgen05.mma (M = 128,
 // N = 128, K = 16, BF16 in, FP32 accumulate) and frees each stage with
-// tcgen05.commit; after the last k-block all four warps read the accumulator
-// back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = tile rows) and run
-// a fused epilogue:
+// tcgen05.commit; after the last k-block the 16 warps read the accumulator
+// back with tcgen05.ld (warp w: TMEM lanes 32(w % 4)..+31 = tile rows,
+// columns 32(w / 4)..+31) and run a fused epilogue:
 //   EPI_STORE_F32  C = A B^T in FP32 (tests, gradient export)
 //   EPI_BIAS_GELU  forward hidden layer: Z = acc + b, A = gelu(Z); stores Z, A
 //                  and A^T (BF16) so every later GEMM reads K-major operands
@@ -44,7 +44,10 @@ int set_error(int code, const std::string &msg);
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4, GEMM_THREADS = 128;
+// 16 warps: warp w reads TMEM lane quarter w % 4 (tile rows 32(w % 4)..+31)
+// and runs the epilogue of column group w / 4 (32 columns), so the
+// epilogue's transcendental work and stores spread over 4x more warps
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4, GEMM_THREADS = 512;
 constexpr int TILE_BYTES = BM * BK * 2;  // 16 KB per operand per stage
 constexpr int GEMM_SMEM = 1024 + STAGES * 2 * TILE_BYTES + 256;
 constexpr uint64_t kWaitLimitNs = 1000000000ull;  // 1 s
@@ -341,12 +344,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   have = __all_sync(0xffffffffu, have && !*abort && !failed);
   tc_fence_after();
   if (have) {
-#pragma unroll 1
-    for (int c = 0; c < BN / 32; ++c) {
-      float v[32];
-      tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + c * 32, v);
-      epilogue<EPI>(ep, m0 + warp * 32 + lane, n0 + c * 32, v);
-    }
+    const int quarter = warp & 3, group = warp >> 2;
+    float v[32];
+    tmem_ld32(tmem + (static_cast<uint32_t>(quarter * 32) << 16) + group * 32, v);
+    epilogue<EPI>(ep, m0 + quarter * 32 + lane, n0 + group * 32, v);
   } else if (lane == 0) {
     atomicOr(ep.err, 1);
   }
@@ -359,80 +360,85 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 }
 
 // ---- small kernels -------------------------------------------------------------
-// fp32 features [B][in] -> BF16 X [B][in_pad] (zero padded) and X^T [in_pad][B]
-__global__ void pack_input_kernel(const float *x, int B, int in, int in_pad, __nv_bfloat16 *X,
-                                  __nv_bfloat16 *XT) {
-  const int total = B * in_pad;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-    const int c = i % in_pad, r = i / in_pad;
-    const __nv_bfloat16 v = __float2bfloat16_rn(c < in ? x[static_cast<size_t>(r) * in + c] : 0.0f);
-    X[i] = v;
+// fp32 features [B][in] -> BF16 X [B][in_pad] (zero padded) and X^T
+// [in_pad][B]; one block per 32 rows, the transpose through shared memory.
+__global__ void __launch_bounds__(256) pack_input_kernel(const float *x, int B, int in, int in_pad,
+                                                         __nv_bfloat16 *X, __nv_bfloat16 *XT) {
+  __shared__ __nv_bfloat16 tile[128][34];
+  const int r0 = blockIdx.x * 32;
+  for (int i = threadIdx.x; i < 32 * in_pad; i += 256) {
+    const int rr = i / in_pad, c = i % in_pad;
+    const __nv_bfloat16 v =
+        __float2bfloat16_rn(c < in ? x[static_cast<size_t>(r0 + rr) * in + c] : 0.0f);
+    X[static_cast<size_t>(r0 + rr) * in_pad + c] = v;
+    tile[c][rr] = v;
   }
-  // transposed copy, row-contiguous in B
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-    const int r = i % B, c = i / B;
-    XT[i] = __float2bfloat16_rn(c < in ? x[static_cast<size_t>(r) * in + c] : 0.0f);
+  __syncthreads();
+  for (int i = threadIdx.x; i < 32 * in_pad; i += 256) {
+    const int c = i / 32, rr = i % 32;
+    XT[static_cast<size_t>(c) * B + r0 + rr] = tile[c][rr];
   }
 }
 
-// Output layer and loss: y = A3 w4 + b4; with targets, dy = 2 (y - t) / B,
-// sum (y - t)^2 into *loss, and dZ3 = dy w4 * gelu'(Z3) in both orientations.
-// One block of 256 threads per 32 rows.
-__global__ void __launch_bounds__(256) head_kernel(const __nv_bfloat16 *A3, const __nv_bfloat16 *Z3,
-                                                   const float *w4, const float *b4, int B, int H,
-                                                   const float *target, float *y, float *dy,
-                                                   float *loss, __nv_bfloat16 *dZ3,
-                                                   __nv_bfloat16 *dZ3T) {
-  __shared__ float s_dy[32];
-  __shared__ __nv_bfloat16 tile[64][34];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r0 = blockIdx.x * 32;
-  float part = 0.0f;
-  for (int rr = warp; rr < 32; rr += 8) {
-    const int r = r0 + rr;
-    float acc = 0.0f;
-    if (r < B)
-      for (int c = lane; c < H; c += 32)
-        acc += __bfloat162float(A3[static_cast<size_t>(r) * H + c]) * w4[c];
+// Output layer and loss: y = A3 w4 + b4, one warp per row (8 BF16 per lane
+// per load); with targets, dy = 2 (y - t) / B and sum (y - t)^2 into *loss.
+__global__ void __launch_bounds__(256) head_y_kernel(const __nv_bfloat16 *A3, const float *w4,
+                                                     const float *b4, int B, int H,
+                                                     const float *target, float *y, float *dy,
+                                                     float *loss) {
+  __shared__ float s_loss[8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // the grid covers B exactly
+  const uint4 *row = reinterpret_cast<const uint4 *>(A3 + static_cast<size_t>(r) * H);
+  float acc = 0.0f;
+  for (int j = lane; j < H / 8; j += 32) {
+    const uint4 u = row[j];
+    const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&u);
 #pragma unroll
-    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    const float yr = acc + b4[0];
-    if (lane == 0) {
-      float d = 0.0f;
-      if (r < B) {
-        y[r] = yr;
-        if (target) {
-          const float e = yr - target[r];
-          d = 2.0f * e / static_cast<float>(B);
-          part += e * e;
-          dy[r] = d;
-        }
-      }
-      s_dy[rr] = d;
-    }
+    for (int q = 0; q < 8; ++q) acc += __bfloat162float(h[q]) * w4[8 * j + q];
   }
-  if (lane == 0 && target && part != 0.0f) atomicAdd(loss, part);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    const float yr = acc + b4[0];
+    y[r] = yr;
+    float e2 = 0.0f;
+    if (target) {
+      const float e = yr - target[r];
+      dy[r] = 2.0f * e / static_cast<float>(B);
+      e2 = e * e;
+    }
+    s_loss[wid] = e2;
+  }
   if (!target) return;
   __syncthreads();
-  // dZ3 for the block's 32 rows, 64 columns at a time
-  for (int c0 = 0; c0 < H; c0 += 64) {
-    for (int i = threadIdx.x; i < 32 * 64; i += 256) {
-      const int rr = i / 64, cc = i % 64;
-      const int r = r0 + rr, c = c0 + cc;
-      __nv_bfloat16 g = __float2bfloat16_rn(0.0f);
-      if (r < B) {
-        const float z = __bfloat162float(Z3[static_cast<size_t>(r) * H + c]);
-        g = __float2bfloat16_rn(s_dy[rr] * w4[c] * gelu_grad(z));
-        dZ3[static_cast<size_t>(r) * H + c] = g;
-      }
-      tile[cc][rr] = g;
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 32 * 64; i += 256) {
-      const int cc = i / 32, rr = i % 32;
-      if (r0 + rr < B) dZ3T[static_cast<size_t>(c0 + cc) * B + r0 + rr] = tile[cc][rr];
-    }
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t += s_loss[i];
+    atomicAdd(loss, t);
+  }
+}
+
+// dZ3 = dy w4 * gelu'(Z3) for a 32-row x 64-column tile per block, stored in
+// both orientations (the transposed copy through shared memory).
+__global__ void __launch_bounds__(256) head_dz_kernel(const __nv_bfloat16 *Z3, const float *w4,
+                                                      const float *dy, int B, int H,
+                                                      __nv_bfloat16 *dZ3, __nv_bfloat16 *dZ3T) {
+  __shared__ __nv_bfloat16 tile[64][34];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 64;
+  for (int i = threadIdx.x; i < 32 * 64; i += 256) {
+    const int rr = i / 64, cc = i % 64;
+    const int r = r0 + rr, c = c0 + cc;
+    const float z = __bfloat162float(Z3[static_cast<size_t>(r) * H + c]);
+    const __nv_bfloat16 g = __float2bfloat16_rn(dy[r] * w4[c] * gelu_grad(z));
+    dZ3[static_cast<size_t>(r) * H + c] = g;
+    tile[cc][rr] = g;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 32 * 64; i += 256) {
+    const int cc = i / 32, rr = i % 32;
+    dZ3T[static_cast<size_t>(c0 + cc) * B + r0 + rr] = tile[cc][rr];
   }
 }
 
@@ -467,10 +473,22 @@ __global__ void vec_adam_kernel(VecAdam p0, VecAdam p1, VecAdam p2, VecAdam p3, 
   }
   float g = 0.0f;
   if (p.rows) {
-    const __nv_bfloat16 *row = p.rows + static_cast<size_t>(idx) * B;
-    for (int j = lane; j < B; j += 32) {
-      const float x = __bfloat162float(row[j]);
-      g += p.dy ? x * p.dy[j] : x;
+    // B is a multiple of 128: 8 BF16 (16 bytes) per lane per load
+    const uint4 *row = reinterpret_cast<const uint4 *>(p.rows + static_cast<size_t>(idx) * B);
+    for (int j = lane; j < B / 8; j += 32) {
+      const uint4 u = row[j];
+      const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&u);
+      if (p.dy) {
+        const float4 d0 = reinterpret_cast<const float4 *>(p.dy)[2 * j];
+        const float4 d1 = reinterpret_cast<const float4 *>(p.dy)[2 * j + 1];
+        g += __bfloat162float(h[0]) * d0.x + __bfloat162float(h[1]) * d0.y +
+             __bfloat162float(h[2]) * d0.z + __bfloat162float(h[3]) * d0.w +
+             __bfloat162float(h[4]) * d1.x + __bfloat162float(h[5]) * d1.y +
+             __bfloat162float(h[6]) * d1.z + __bfloat162float(h[7]) * d1.w;
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) g += __bfloat162float(h[q]);
+      }
     }
   } else {
     for (int j = lane; j < B; j += 32) g += p.dy[j];
@@ -546,45 +564,43 @@ cudaError_t launch_gemm(const CUtensorMap &a, const CUtensorMap &b, int M, int N
 
 // Sum of the split-K partial tiles of a weight gradient g[M][N] in a fixed
 // order, then either the Adam update (FP32 master, moments, BF16 W and W^T)
-// or, with grad_out, the gradient itself.  32 x 32 tiles, 256 threads; W^T
-// goes through shared memory so both stores are coalesced.
-__global__ void __launch_bounds__(256) adam_reduce_kernel(const float *__restrict__ part, int splits,
-                                                          int M, int N, float *w, float *m,
-                                                          float *v, __nv_bfloat16 *w_bf,
-                                                          __nv_bfloat16 *w_bf_t, float *grad_out,
-                                                          float lr, float beta1, float beta2,
-                                                          float eps, float bc1, float bc2) {
+// or, with grad_out, the gradient itself.  One element per thread, 32 x 32
+// tiles of 1024 threads; W^T goes through shared memory so both stores are
+// coalesced.
+__global__ void __launch_bounds__(1024) adam_reduce_kernel(const float *__restrict__ part,
+                                                           int splits, int M, int N, float *w,
+                                                           float *m, float *v,
+                                                           __nv_bfloat16 *w_bf,
+                                                           __nv_bfloat16 *w_bf_t, float *grad_out,
+                                                           float lr, float beta1, float beta2,
+                                                           float eps, float bc1, float bc2) {
   __shared__ __nv_bfloat16 tile[32][34];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const int r = blockIdx.y * 32 + ty, c = blockIdx.x * 32 + tx;
   const size_t MN = static_cast<size_t>(M) * N;
+  const size_t k = static_cast<size_t>(r) * N + c;
+  float pz[8];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int r = r0 + ty + 8 * i, c = c0 + tx;
-    const size_t k = static_cast<size_t>(r) * N + c;
-    float g = part[k];
-    for (int z = 1; z < splits; ++z) g += part[z * MN + k];
-    if (grad_out) {
-      grad_out[k] = g;
-      continue;
-    }
-    const float mm = beta1 * m[k] + (1.0f - beta1) * g;
-    const float vv = beta2 * v[k] + (1.0f - beta2) * g * g;
-    const float ww = w[k] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
-    m[k] = mm;
-    v[k] = vv;
-    w[k] = ww;
-    const __nv_bfloat16 wb = __float2bfloat16_rn(ww);
-    w_bf[k] = wb;
-    tile[tx][ty + 8 * i] = wb;
+  for (int z = 0; z < 8; ++z) pz[z] = z < splits ? part[z * MN + k] : 0.0f;
+  float g = pz[0];
+#pragma unroll
+  for (int z = 1; z < 8; ++z)
+    if (z < splits) g += pz[z];
+  if (grad_out) {
+    grad_out[k] = g;
+    return;
   }
-  if (grad_out) return;
+  const float mm = beta1 * m[k] + (1.0f - beta1) * g;
+  const float vv = beta2 * v[k] + (1.0f - beta2) * g * g;
+  const float ww = w[k] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+  m[k] = mm;
+  v[k] = vv;
+  w[k] = ww;
+  const __nv_bfloat16 wb = __float2bfloat16_rn(ww);
+  w_bf[k] = wb;
+  tile[tx][ty] = wb;
   __syncthreads();
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int c = c0 + ty + 8 * i, r = r0 + tx;
-    w_bf_t[static_cast<size_t>(c) * M + r] = tile[ty + 8 * i][tx];
-  }
+  w_bf_t[static_cast<size_t>(blockIdx.x * 32 + ty) * M + blockIdx.y * 32 + tx] = tile[ty][tx];
 }
 
 template <typename T>
@@ -702,9 +718,10 @@ int backward(emt6_mlp *net, int B, const float *d_target, bool apply, float lr) 
   float *loss = net->loss.p;
   e = cudaMemsetAsync(loss, 0, sizeof(float), st);
   if (e != cudaSuccess) return cuda_fail(e, "surrogate");
-  head_kernel<<<B / 32, 256, 0, st>>>(net->A[2].p, net->Z[2].p, net->w4.p, net->b4.p, B, net->H,
-                                      d_target, net->y.p, net->dy.p, loss, net->dZ[2].p,
-                                      net->dZT[2].p);
+  head_y_kernel<<<B / 8, 256, 0, st>>>(net->A[2].p, net->w4.p, net->b4.p, B, net->H, d_target,
+                                        net->y.p, net->dy.p, loss);
+  head_dz_kernel<<<dim3(B / 32, net->H / 64), 256, 0, st>>>(net->Z[2].p, net->w4.p, net->dy.p, B,
+                                                            net->H, net->dZ[2].p, net->dZT[2].p);
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "surrogate head");
   ++net->step;
   const float bc1 = 1.0f - std::pow(net->beta1, static_cast<float>(net->step));
@@ -729,7 +746,7 @@ int backward(emt6_mlp *net, int B, const float *d_target, bool apply, float lr) 
       ep.c_out = net->work.p;
       e = launch_gemm<EPI_STORE_F32>(net->mdZT[l], bmap, net->H, N, B, ep, st, splits);
       if (e == cudaSuccess) {
-        adam_reduce_kernel<<<dim3(N / 32, net->H / 32), 256, 0, st>>>(
+        adam_reduce_kernel<<<dim3(N / 32, net->H / 32), 1024, 0, st>>>(
             net->work.p, splits, net->H, N, net->w[l].p, net->m[l].p, net->v[l].p, net->wb[l].p,
             net->wbt[l].p, apply ? nullptr : net->gradw[l].p, lr, net->beta1, net->beta2,
             net->eps, bc1, bc2);
@@ -774,8 +791,8 @@ int backward(emt6_mlp *net, int B, const float *d_target, bool apply, float lr) 
 }
 
 int pack(emt6_mlp *net, const float *d_x, int B) {
-  pack_input_kernel<<<304, 256, 0, net->stream>>>(d_x, B, net->in, net->in_pad, net->X.p,
-                                                   net->XT.p);
+  pack_input_kernel<<<B / 32, 256, 0, net->stream>>>(d_x, B, net->in, net->in_pad, net->X.p,
+                                                      net->XT.p);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? EMT6_OK : cuda_fail(e, "surrogate input");
 }
@@ -927,9 +944,8 @@ int emt6_mlp_predict(emt6_mlp *net, const float *d_x, int B, float *d_y) {
   if (rc == EMT6_OK) rc = pack(net, d_x, B);
   if (rc == EMT6_OK) rc = forward_hidden(net, B);
   if (rc != EMT6_OK) return rc;
-  head_kernel<<<B / 32, 256, 0, net->stream>>>(net->A[2].p, net->Z[2].p, net->w4.p, net->b4.p, B,
-                                                net->H, nullptr, d_y, nullptr, nullptr, nullptr,
-                                                nullptr);
+  head_y_kernel<<<B / 8, 256, 0, net->stream>>>(net->A[2].p, net->w4.p, net->b4.p, B, net->H,
+                                                  nullptr, d_y, nullptr, nullptr);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? EMT6_OK : cuda_fail(e, "emt6_mlp_predict");
 }
