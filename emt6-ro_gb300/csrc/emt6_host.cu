@@ -492,6 +492,43 @@ __global__ void count_kernel(const uint8_t *st, uint32_t sstride, int HW, uint32
   }
 }
 
+// Per simulation, 13 floats: cho, ox, gi at the centre site (H/2, W/2), the
+// living count, occupied sites per metabolic mode (4) and per cycle phase (5)
+// (the quantities example/timelapse.cc records, computed on the device).
+__global__ void summary_kernel(const float *fld, uint32_t fstride, const uint8_t *st,
+                               uint32_t sstride, const float4 *cell, int H, int W, float *out,
+                               int64_t n) {
+  __shared__ int part[8][10];
+  const int HW = H * W, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int64_t sim = blockIdx.x; sim < n; sim += gridDim.x) {
+    const uint8_t *s = st + sim * sstride;
+    const float4 *c = cell + sim * (int64_t)HW * 3;
+    int cnt[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int q = threadIdx.x; q < HW; q += blockDim.x) {
+      if ((s[q] & 3) != 1) continue;
+      const uint32_t mp = __float_as_uint(c[3 * q + 2].y);
+      cnt[0] += 1;
+      cnt[1 + (mp & 3)] += 1;
+      cnt[5 + min((int)((mp >> 8) & 0xff), 4)] += 1;
+    }
+#pragma unroll
+    for (int k = 0; k < 10; ++k)
+      for (int o = 16; o; o >>= 1) cnt[k] += __shfl_xor_sync(0xffffffffu, cnt[k], o);
+    if (lane == 0)
+      for (int k = 0; k < 10; ++k) part[wid][k] = cnt[k];
+    __syncthreads();
+    if (threadIdx.x < 10) {
+      int t = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w][threadIdx.x];
+      out[sim * 13 + 3 + threadIdx.x] = (float)t;
+    } else if (threadIdx.x < 13) {
+      const int f = threadIdx.x - 10;
+      out[sim * 13 + f] = fld[sim * fstride + (int64_t)f * HW + (H / 2) * W + W / 2];
+    }
+    __syncthreads();
+  }
+}
+
 void site_to_records(const emt6_site &s, float *fld3, uint8_t *stv, float4 *cell3) {
   fld3[0] = s.cho;
   fld3[1] = s.ox;
@@ -841,6 +878,23 @@ int emt6_batch_counts(emt6_batch *b, uint32_t *out) {
   EMT6_CUDA(cudaGetLastError());
   b->launches += 1;
   EMT6_CUDA(cudaMemcpyAsync(out, b->counts.p, b->n * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            b->stream));
+  EMT6_CUDA(cudaStreamSynchronize(b->stream));
+  return b->check_err();
+}
+
+int emt6_batch_summary(emt6_batch *b, float *out) {
+  if (!b || !out) return fail(EMT6_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(b->mu);
+  DeviceGuard g(b->device);
+  DevBuf<float> d;
+  EMT6_CUDA(d.alloc((size_t)b->n * 13));
+  const int grid = (int)std::min<int64_t>(b->n, 65535 * 4);
+  summary_kernel<<<grid, 256, 0, b->stream>>>(b->fld.p, b->fstride, b->st.p, b->sstride,
+                                              b->cell.p, b->H, b->W, d.p, b->n);
+  EMT6_CUDA(cudaGetLastError());
+  b->launches += 1;
+  EMT6_CUDA(cudaMemcpyAsync(out, d.p, (size_t)b->n * 13 * sizeof(float), cudaMemcpyDeviceToHost,
                             b->stream));
   EMT6_CUDA(cudaStreamSynchronize(b->stream));
   return b->check_err();

@@ -337,60 +337,8 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
     const uint32_t u0 = fin ? rm0 : fm0;
     const uint32_t u1 = fin ? rm1 : fm1;
     const int par = s & 1;
-    if constexpr (NP == 2 && !WIDE && RH <= 14) {
-      // all horizontal sums of the substep first: 2*RH independent shuffles
-      float h0[RH];
-#pragma unroll
-      for (int i = 0; i < RH; ++i)
-        h0[i] = __shfl_sync(kFull, x0[i], left) + __shfl_sync(kFull, x0[i], right);
-      // Producer/consumer exchange with the partner warp: publish the
-      // boundary row's G, arrive on this part's barrier, update every row that
-      // does not need the partner, then wait on the partner's barrier for its
-      // G.  Barrier ids alternate with the substep parity so a warp that runs
-      // a substep ahead never arrives twice on one barrier instance.
-      const int own = bar_id + par * 2 + part, other = bar_id + par * 2 + (1 - part);
-      if (part == 0) {
-        const float gl = fmaf(cd, h0[RH - 1], cb * x0[RH - 1]);
-        *slot(par, 0, 1) = gl;
-        named_arrive(own, 64);
-        float gm = top_g();
-        float gc = RH > 1 ? fmaf(cd, h0[0], cb * x0[0]) : gl;
-#pragma unroll
-        for (int i = 0; i < RH - 1; ++i) {
-          const float gn = (i + 1 == RH - 1) ? gl : fmaf(cd, h0[i + 1], cb * x0[i + 1]);
-          const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i], gm + gn));
-          if ((u0 >> i) & 1u) x0[i] = nv0;
-          gm = gc;
-          gc = gn;
-        }
-        named_barrier(other, 64);
-        const float gx = *slot(par, 1, 0);
-        const float nv0 = fmaf(ca, x0[RH - 1], fmaf(cb, h0[RH - 1], gm + gx));
-        if ((u0 >> (RH - 1)) & 1u) x0[RH - 1] = nv0;
-      } else {
-        const float gf = fmaf(cd, h0[0], cb * x0[0]);
-        *slot(par, 1, 0) = gf;
-        named_arrive(own, 64);
-        const float x_first = x0[0];
-        // G of row 1, taken before the loop overwrites x0[1]
-        const float g_second = RH > 1 ? fmaf(cd, h0[RH > 1 ? 1 : 0], cb * x0[RH > 1 ? 1 : 0]) : 0.f;
-        float gm = gf, gc = g_second;
-#pragma unroll
-        for (int i = 1; i < RH; ++i) {
-          const float gn = (i + 1 < RH) ? fmaf(cd, h0[i + 1], cb * x0[i + 1]) : 0.f;
-          const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i], gm + gn));
-          if ((u0 >> i) & 1u) x0[i] = nv0;
-          gm = gc;
-          gc = gn;
-        }
-        named_barrier(other, 64);
-        const float gp = *slot(par, 0, 1);
-        const float nv0 = fmaf(ca, x_first, fmaf(cb, h0[0], gp + g_second));
-        if (u0 & 1u) x0[0] = nv0;
-      }
-    } else if constexpr (!WIDE) {
-      // RH 15-16: horizontal sums on the fly (the two-phase form needs RH more
-      // registers than the narrow kernel's budget)
+    if constexpr (!WIDE) {
+      // four warps per field, one column per lane: horizontal sums on the fly
       const float ht0 = __shfl_sync(kFull, x0[0], left) + __shfl_sync(kFull, x0[0], right);
       const float hb0 =
           __shfl_sync(kFull, x0[RH - 1], left) + __shfl_sync(kFull, x0[RH - 1], right);
@@ -477,6 +425,131 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
   }
 }
 
+// Two-warp narrow layout with two columns per lane: the 16 lanes of each
+// half-warp cover columns 2*hl + coff and 2*hl + 1 + coff (32 columns), the
+// half-warps split the warp's rows, so the four half-warps of a field hold
+// bands of R rows (band = 2 * part + half).  A horizontal sum costs one
+// shuffle per site instead of two; the bands of one warp swap boundary G by
+// a shuffle across the half-warps, the two warps through shared memory with
+// the same producer/consumer barriers as diffuse_part.  Same sites, same
+// expressions as diffuse_part, so the results are bit-identical.
+template <int R>
+__device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t *__restrict__ colmask,
+                                          float4 *__restrict__ xch, int part, int r0, int c0,
+                                          int h, int w, int nrow, int ncol, int W, float ext,
+                                          float ca, float cb, float cd, int nfree, int bar_id,
+                                          int roff, int coff) {
+  const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+  const int band = part * 2 + half;
+  const int base = band * R + roff;  // region row of register row 0
+  const int j0 = 2 * hl + coff, j1 = j0 + 1;
+  const int left = (lane & 16) | ((hl + 15) & 15), right = (lane & 16) | ((hl + 1) & 15);
+  const uint32_t rowsel = (1u << R) - 1u;
+  const uint32_t fm0 = (j0 < ncol) ? (uint32_t)(colmask[j0] >> base) & rowsel : 0u;
+  const uint32_t fm1 = (j1 < ncol) ? (uint32_t)(colmask[j1] >> base) & rowsel : 0u;
+  const uint32_t roirows = (uint32_t)(((((1ull << h) - 1ull) << 1)) >> base) & rowsel;
+  const uint32_t rm0 = (j0 >= 1 && j0 <= w) ? roirows : 0u;
+  const uint32_t rm1 = (j1 >= 1 && j1 <= w) ? roirows : 0u;
+  const int lat0 = (r0 - 1) * W + (c0 - 1);
+  // G of the row above band 0: the zero ring, or region row 0 held at the
+  // external level when the mapping starts at row 1
+  float top0 = 0.f, top1 = 0.f;
+  if (roff) {
+    const float tx0 = (j0 < ncol) ? ext : 0.f, tx1 = (j1 < ncol) ? ext : 0.f;
+    const float th0 = ((j0 - 1 >= 0 && j0 - 1 < ncol) ? ext : 0.f) + tx1;
+    const float th1 = tx0 + ((j1 + 1 < ncol) ? ext : 0.f);
+    top0 = fmaf(cd, th0, cb * tx0);
+    top1 = fmaf(cd, th1, cb * tx1);
+  }
+  float x0[R], x1[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int gi = base + i;
+    const bool inr = gi < nrow;
+    x0[i] = (inr && j0 < ncol) ? (((fm0 >> i) & 1u) ? f[lat0 + gi * W + j0] : ext) : 0.f;
+    x1[i] = (inr && j1 < ncol) ? (((fm1 >> i) & 1u) ? f[lat0 + gi * W + j1] : ext) : 0.f;
+  }
+  // boundary G between the two warps: slot 0 = part 0's last row (written by
+  // its second half-warp), slot 1 = part 1's first row (its first half-warp)
+  float2 *xs = reinterpret_cast<float2 *>(xch);
+  const bool writes = (part == 0) ? half == 1 : half == 0;
+  for (int s = 0; s <= nfree; ++s) {
+    const bool fin = (s == nfree);
+    const uint32_t u0 = fin ? rm0 : fm0;
+    const uint32_t u1 = fin ? rm1 : fm1;
+    const int par = s & 1;
+    float h0[R], h1[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      h0[i] = __shfl_sync(kFull, x1[i], left) + x1[i];
+      h1[i] = x0[i] + __shfl_sync(kFull, x0[i], right);
+    }
+    const float gf0 = fmaf(cd, h0[0], cb * x0[0]), gf1 = fmaf(cd, h1[0], cb * x1[0]);
+    const float gl0 = fmaf(cd, h0[R - 1], cb * x0[R - 1]);
+    const float gl1 = fmaf(cd, h1[R - 1], cb * x1[R - 1]);
+    // the first half-warp sends its last row's G, the second its first row's
+    const float rc0 = __shfl_xor_sync(kFull, half ? gf0 : gl0, 16);
+    const float rc1 = __shfl_xor_sync(kFull, half ? gf1 : gl1, 16);
+    const int own = bar_id + par * 2 + part, other = bar_id + par * 2 + (1 - part);
+    if (writes) xs[(par * 2 + part) * 16 + hl] = part == 0 ? make_float2(gl0, gl1)
+                                                           : make_float2(gf0, gf1);
+    named_arrive(own, 64);
+    // rows 1 .. R-2 need only this band's G
+    float gm0 = gf0, gm1 = gf1;
+    float gc0 = R > 1 ? fmaf(cd, h0[R > 1 ? 1 : 0], cb * x0[R > 1 ? 1 : 0]) : 0.f;
+    float gc1 = R > 1 ? fmaf(cd, h1[R > 1 ? 1 : 0], cb * x1[R > 1 ? 1 : 0]) : 0.f;
+    const float g_second0 = gc0, g_second1 = gc1;
+#pragma unroll
+    for (int i = 1; i < R - 1; ++i) {
+      const float gn0 = (i + 1 == R - 1) ? gl0 : fmaf(cd, h0[i + 1], cb * x0[i + 1]);
+      const float gn1 = (i + 1 == R - 1) ? gl1 : fmaf(cd, h1[i + 1], cb * x1[i + 1]);
+      const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i], gm0 + gn0));
+      const float nv1 = fmaf(ca, x1[i], fmaf(cb, h1[i], gm1 + gn1));
+      if ((u0 >> i) & 1u) x0[i] = nv0;
+      if ((u1 >> i) & 1u) x1[i] = nv1;
+      gm0 = gc0;
+      gm1 = gc1;
+      gc0 = gn0;
+      gc1 = gn1;
+    }
+    // G of the row before the last (rows 0 .. R-2 are not yet overwritten at
+    // their G's computation): the loop leaves it in gm when R > 2
+    const float g_penult0 = R > 2 ? gm0 : gf0, g_penult1 = R > 2 ? gm1 : gf1;
+    named_barrier(other, 64);
+    float2 pw = make_float2(0.f, 0.f);
+    if (writes) pw = xs[(par * 2 + (1 - part)) * 16 + hl];
+    // above the first row, below the last row
+    const float ab0 = band == 0 ? top0 : (half ? rc0 : pw.x);
+    const float ab1 = band == 0 ? top1 : (half ? rc1 : pw.y);
+    const float be0 = band == 3 ? 0.f : (half ? pw.x : rc0);
+    const float be1 = band == 3 ? 0.f : (half ? pw.y : rc1);
+    if (R == 1) {
+      const float nv0 = fmaf(ca, x0[0], fmaf(cb, h0[0], ab0 + be0));
+      const float nv1 = fmaf(ca, x1[0], fmaf(cb, h1[0], ab1 + be1));
+      if (u0 & 1u) x0[0] = nv0;
+      if (u1 & 1u) x1[0] = nv1;
+    } else {
+      const float f0 = fmaf(ca, x0[0], fmaf(cb, h0[0], ab0 + g_second0));
+      const float f1 = fmaf(ca, x1[0], fmaf(cb, h1[0], ab1 + g_second1));
+      const float l0 = fmaf(ca, x0[R - 1], fmaf(cb, h0[R - 1], g_penult0 + be0));
+      const float l1 = fmaf(ca, x1[R - 1], fmaf(cb, h1[R - 1], g_penult1 + be1));
+      if (u0 & 1u) x0[0] = f0;
+      if (u1 & 1u) x1[0] = f1;
+      if ((u0 >> (R - 1)) & 1u) x0[R - 1] = l0;
+      if ((u1 >> (R - 1)) & 1u) x1[R - 1] = l1;
+    }
+  }
+  // write back the ROI interior
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int gi = base + i;
+    if (gi >= 1 && gi <= h) {
+      if (j0 >= 1 && j0 <= w) f[lat0 + gi * W + j0] = x0[i];
+      if (j1 >= 1 && j1 <= w) f[lat0 + gi * W + j1] = x1[i];
+    }
+  }
+}
+
 // NP warps per field; warp w diffuses field w / NP, part w % NP.
 // The caller guarantees 2*NP*RH_max >= nrow and (WIDE_OK or ncol <= 31).
 template <int NP, bool WIDE_OK>
@@ -488,8 +561,7 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
   const int wid = threadIdx.x >> 5;
   const int field = wid / NP, part = wid % NP;
   const int roff = NP == 2 ? m->roff : 0, coff = NP == 2 ? m->coff : 0;
-  int RH = (nrow - roff + NP - 1) / NP;
-  if (NP != 2) RH = (RH + 1) & ~1;  // the two-warp path takes any row count
+  const int RH = (((nrow - roff + NP - 1) / NP) + 1) & ~1;  // four-warp path: even rows
   float *f = fld + field * p.HW;
   float4 *x = xch + field * 2 * NP * (NP == 2 ? 1 : 2) * 32;
   const float ext = p.ext[field], ca = p.da[field], cb = p.db[field], cd = p.dd[field];
@@ -499,32 +571,35 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
 #define EMT6_CALL(R, WD)                                                                   \
   diffuse_part<NP, R, WD>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, \
                           nf, bar, roff, coff)
-#define EMT6_CASES(WD)                                    \
-  switch (RH) {                                           \
-    case 2: EMT6_CALL(2, WD); break;                      \
-    case 4: EMT6_CALL(4, WD); break;                      \
-    case 6: EMT6_CALL(6, WD); break;                      \
-    case 8: EMT6_CALL(8, WD); break;                      \
-    case 10: EMT6_CALL(10, WD); break;                    \
-    case 12: EMT6_CALL(12, WD); break;                    \
-    case 14: EMT6_CALL(14, WD); break;                    \
-    default:                                              \
-      if constexpr (NP == 2 && !WD) {                     \
-        switch (RH) {                                     \
-          case 3: EMT6_CALL(3, false); break;             \
-          case 5: EMT6_CALL(5, false); break;             \
-          case 7: EMT6_CALL(7, false); break;             \
-          case 9: EMT6_CALL(9, false); break;             \
-          case 11: EMT6_CALL(11, false); break;           \
-          case 13: EMT6_CALL(13, false); break;           \
-          case 15: EMT6_CALL(15, false); break;           \
-          case 16: EMT6_CALL(16, false); break;           \
-          default: break;                                 \
-        }                                                 \
-      }                                                   \
-      break;                                              \
+#define EMT6_CASES(WD)               \
+  switch (RH) {                      \
+    case 2: EMT6_CALL(2, WD); break;   \
+    case 4: EMT6_CALL(4, WD); break;   \
+    case 6: EMT6_CALL(6, WD); break;   \
+    case 8: EMT6_CALL(8, WD); break;   \
+    case 10: EMT6_CALL(10, WD); break; \
+    case 12: EMT6_CALL(12, WD); break; \
+    case 14: EMT6_CALL(14, WD); break; \
+    default: break;                    \
   }
-  if (!WIDE_OK || ncol <= 31) {
+  if constexpr (NP == 2) {
+    // narrow kernel: two columns per lane, four bands of R rows per field
+    const int R = (nrow - roff + 3) / 4;
+#define EMT6_HALF(RR) \
+  diffuse_half<RR>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf, bar, roff, coff)
+    switch (R) {
+      case 1: EMT6_HALF(1); break;
+      case 2: EMT6_HALF(2); break;
+      case 3: EMT6_HALF(3); break;
+      case 4: EMT6_HALF(4); break;
+      case 5: EMT6_HALF(5); break;
+      case 6: EMT6_HALF(6); break;
+      case 7: EMT6_HALF(7); break;
+      case 8: EMT6_HALF(8); break;
+      default: break;
+    }
+#undef EMT6_HALF
+  } else if (!WIDE_OK || ncol <= 31) {
     EMT6_CASES(false)
   } else {
     EMT6_CASES(WIDE_OK)

@@ -80,6 +80,7 @@ _SIGNATURES = {
     "emt6_batch_sync": (_c.c_int, [_VP]),
     "emt6_batch_counts": (_c.c_int, [_VP, _VP]),
     "emt6_batch_get_state": (_c.c_int, [_VP, _c.c_int64, _VP]),
+    "emt6_batch_summary": (_c.c_int, [_VP, _VP]),
     "emt6_batch_step": (_c.c_int, [_VP, _c.c_int64, _P(_c.c_uint32)]),
     "emt6_batch_stream": (_VP, [_VP]),
     "emt6_batch_diffused": (_c.c_int, [_VP, _P(_c.c_ulonglong)]),

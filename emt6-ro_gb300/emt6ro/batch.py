@@ -70,6 +70,26 @@ class Batch:
         N.check(N.lib().emt6_batch_counts(self._h, N.ptr(out)))
         return out
 
+    SUMMARY_FIELDS = ("cho", "ox", "gi", "living", "mode0", "mode1", "mode2", "mode3",
+                      "g1", "s", "g2", "m", "d")
+
+    def summary(self) -> np.ndarray:
+        """(n, 13) float32 per simulation: centre-site cho, ox, gi, living
+        cells, living cells per metabolic mode (4) and per phase (5)."""
+        out = np.zeros((self.n, 13), np.float32)
+        N.check(N.lib().emt6_batch_summary(self._h, N.ptr(out)))
+        return out
+
+    def timelapse(self, steps: int, every: int = 1) -> np.ndarray:
+        """Run `steps` steps, recording `summary()` after every `every` steps
+        (example/timelapse.cc:24-45 records every step on the host); returns
+        (steps // every, n, 13)."""
+        rec = []
+        for _ in range(steps // every):
+            self.run(every)
+            rec.append(self.summary())
+        return np.stack(rec) if rec else np.zeros((0, self.n, 13), np.float32)
+
     def state(self, sim: int) -> TumorState:
         buf = np.zeros((self.H, self.W), dtype=N.SITE_DTYPE)
         N.check(N.lib().emt6_batch_get_state(self._h, int(sim), N.ptr(buf)))

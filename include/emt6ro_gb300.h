@@ -117,6 +117,11 @@ int emt6_batch_sync(emt6_batch *b);
 /* Living-cell count per simulation after the enqueued work
  * (Simulation::getResults + countLiving, statistics.cu:9-38). Blocks. */
 int emt6_batch_counts(emt6_batch *b, uint32_t *out);
+/* Device-side summary after the enqueued work, 13 floats per simulation into
+ * out[n][13]: cho, ox, gi at the centre site (H/2, W/2), living cells, living
+ * cells per metabolic mode (4) and per cycle phase (5) -- the record of
+ * example/timelapse.cc:24-45, without copying lattices to the host. Blocks. */
+int emt6_batch_summary(emt6_batch *b, float *out);
 /* Copy one simulation's lattice to the host (Simulation::getData, simulation.cu:200-206). */
 int emt6_batch_get_state(emt6_batch *b, int64_t sim, emt6_site *out);
 /* Current step counter of one simulation. */

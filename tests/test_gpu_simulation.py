@@ -165,3 +165,30 @@ def test_diffused_counter_matches_oracle(params, oracle):
     sp = np.zeros(2, np.int32)
     b, ob, c, co = _run_pair(params, oracle, tumors, [[]], st, sp, 300, seed=8)
     assert b.diffused() == ob.diffused()
+
+
+def test_summary_and_timelapse_match_oracle_states(params, oracle):
+    """Device-side summaries (centre substrates, living cells, cells per mode
+    and per phase) equal the same quantities computed from the oracle's
+    lattices at every recorded step."""
+    from emt6ro import workloads as wl
+    from emt6ro.batch import Batch
+    tumors = [wl.disc_tumor(params, 9, seed=71), wl.disc_tumor(params, 12, seed=72)]
+    protocols = [[(300, 2.0)], []]
+    st = np.array([0, 1, 1], np.int32)
+    sp = np.array([0, 0, 1], np.int32)
+    b = Batch(params, tumors, protocols, st, sp, seed=17)
+    rec = b.timelapse(900, every=300)
+    assert rec.shape == (3, 3, 13)
+    ob = oracle.Batch(oracle.params_copy(params.native), 3, 17)
+    for i in range(3):
+        ob.set(i, tumors[st[i]].sites, b.doses[sp[i]])
+    for k in range(3):
+        ob.run(300, nthreads=3)
+        for i in range(3):
+            s = ob.get(i).reshape(53, 53)
+            occ = s["state"] == 1
+            want = [s["cho"][26, 26], s["ox"][26, 26], s["gi"][26, 26], occ.sum()]
+            want += [(s["mode"][occ] == m).sum() for m in range(4)]
+            want += [(s["phase"][occ] == ph).sum() for ph in range(5)]
+            assert np.array_equal(rec[k, i], np.array(want, np.float32)), (k, i)
