@@ -33,6 +33,7 @@
 #include <mutex>
 #include <random>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "emt6ro_gb300.h"
@@ -139,6 +140,18 @@ __device__ __forceinline__ void tc_fence_before() {
 
 __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Programmatic dependent launch: the kernels of a training step are launched
+// with programmatic stream serialisation, so each one's launch and prologue
+// overlap the tail of the one before.  pdl_wait() blocks until the previous
+// kernel in the stream has completed and its writes are visible (a no-op
+// without the launch attribute); pdl_trigger(), issued after a CTA's last
+// global write, lets the next kernel be scheduled.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, BF16 inputs, FP32 accumulator.
@@ -297,6 +310,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  pdl_wait();  // operands and epilogue inputs come from the previous kernel
 
   bool failed = false;
   if (threadIdx.x == 0) {
@@ -351,6 +365,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   } else if (lane == 0) {
     atomicOr(ep.err, 1);
   }
+  pdl_trigger();
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
@@ -363,9 +378,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 // fp32 features [B][in] -> BF16 X [B][in_pad] (zero padded) and X^T
 // [in_pad][B]; one block per 32 rows, the transpose through shared memory.
 __global__ void __launch_bounds__(256) pack_input_kernel(const float *x, int B, int in, int in_pad,
-                                                         __nv_bfloat16 *X, __nv_bfloat16 *XT) {
+                                                         __nv_bfloat16 *X, __nv_bfloat16 *XT,
+                                                         float *loss) {
   __shared__ __nv_bfloat16 tile[128][34];
   const int r0 = blockIdx.x * 32;
+  pdl_wait();
+  if (loss && blockIdx.x == 0 && threadIdx.x == 0) *loss = 0.0f;  // this step's loss sum
   for (int i = threadIdx.x; i < 32 * in_pad; i += 256) {
     const int rr = i / in_pad, c = i % in_pad;
     const __nv_bfloat16 v =
@@ -378,6 +396,7 @@ __global__ void __launch_bounds__(256) pack_input_kernel(const float *x, int B, 
     const int c = i / 32, rr = i % 32;
     XT[static_cast<size_t>(c) * B + r0 + rr] = tile[c][rr];
   }
+  pdl_trigger();
 }
 
 // Output layer and loss: y = A3 w4 + b4, one warp per row (8 BF16 per lane
@@ -390,6 +409,7 @@ __global__ void __launch_bounds__(256) head_y_kernel(const __nv_bfloat16 *A3, co
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // the grid covers B exactly
   const uint4 *row = reinterpret_cast<const uint4 *>(A3 + static_cast<size_t>(r) * H);
+  pdl_wait();
   float acc = 0.0f;
   for (int j = lane; j < H / 8; j += 32) {
     const uint4 u = row[j];
@@ -418,6 +438,7 @@ __global__ void __launch_bounds__(256) head_y_kernel(const __nv_bfloat16 *A3, co
     for (int i = 0; i < 8; ++i) t += s_loss[i];
     atomicAdd(loss, t);
   }
+  pdl_trigger();
 }
 
 // dZ3 = dy w4 * gelu'(Z3) for a 32-row x 64-column tile per block, stored in
@@ -427,6 +448,7 @@ __global__ void __launch_bounds__(256) head_dz_kernel(const __nv_bfloat16 *Z3, c
                                                       __nv_bfloat16 *dZ3, __nv_bfloat16 *dZ3T) {
   __shared__ __nv_bfloat16 tile[64][34];
   const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 64;
+  pdl_wait();
   for (int i = threadIdx.x; i < 32 * 64; i += 256) {
     const int rr = i / 64, cc = i % 64;
     const int r = r0 + rr, c = c0 + cc;
@@ -440,6 +462,7 @@ __global__ void __launch_bounds__(256) head_dz_kernel(const __nv_bfloat16 *Z3, c
     const int cc = i / 32, rr = i % 32;
     dZ3T[static_cast<size_t>(c0 + cc) * B + r0 + rr] = tile[cc][rr];
   }
+  pdl_trigger();
 }
 
 struct VecAdam {
@@ -456,6 +479,7 @@ __global__ void vec_adam_kernel(VecAdam p0, VecAdam p1, VecAdam p2, VecAdam p3, 
                                 float lr, float beta1, float beta2, float eps, float bc1, float bc2,
                                 int apply) {
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  pdl_wait();
   int idx = gw;
   VecAdam p;
   if (idx < p0.n) {
@@ -503,6 +527,7 @@ __global__ void vec_adam_kernel(VecAdam p0, VecAdam p1, VecAdam p2, VecAdam p3, 
   p.m[idx] = m;
   p.v[idx] = s;
   p.w[idx] -= lr * (m / bc1) / (sqrtf(s / bc2) + eps);
+  pdl_trigger();
 }
 
 __global__ void to_bf16_kernel(const float *src, __nv_bfloat16 *dst, __nv_bfloat16 *dst_t, int rows,
@@ -544,6 +569,23 @@ bool make_map(CUtensorMap *map, const void *base, int rows, int cols) {
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Launch with programmatic stream serialisation (see pdl_wait / pdl_trigger).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t st, Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 template <int EPI>
 cudaError_t launch_gemm(const CUtensorMap &a, const CUtensorMap &b, int M, int N, int K,
                         const EpiArgs &ep, cudaStream_t st, int splits = 1) {
@@ -557,9 +599,8 @@ cudaError_t launch_gemm(const CUtensorMap &a, const CUtensorMap &b, int M, int N
     if (e != cudaSuccess) return e;
     attr_set[dev] = true;
   }
-  dim3 grid(N / BN, M / BM, splits);
-  mlp_gemm_kernel<EPI><<<grid, GEMM_THREADS, GEMM_SMEM, st>>>(a, b, K / BK / splits, ep);
-  return cudaGetLastError();
+  return launch_pdl(mlp_gemm_kernel<EPI>, dim3(N / BN, M / BM, splits), dim3(GEMM_THREADS),
+                    GEMM_SMEM, st, a, b, K / BK / splits, ep);
 }
 
 // Sum of the split-K partial tiles of a weight gradient g[M][N] in a fixed
@@ -579,6 +620,7 @@ __global__ void __launch_bounds__(1024) adam_reduce_kernel(const float *__restri
   const int r = blockIdx.y * 32 + ty, c = blockIdx.x * 32 + tx;
   const size_t MN = static_cast<size_t>(M) * N;
   const size_t k = static_cast<size_t>(r) * N + c;
+  pdl_wait();
   float pz[8];
 #pragma unroll
   for (int z = 0; z < 8; ++z) pz[z] = z < splits ? part[z * MN + k] : 0.0f;
@@ -601,6 +643,7 @@ __global__ void __launch_bounds__(1024) adam_reduce_kernel(const float *__restri
   tile[tx][ty] = wb;
   __syncthreads();
   w_bf_t[static_cast<size_t>(blockIdx.x * 32 + ty) * M + blockIdx.y * 32 + tx] = tile[ty][tx];
+  pdl_trigger();
 }
 
 template <typename T>
@@ -716,13 +759,15 @@ int backward(emt6_mlp *net, int B, const float *d_target, bool apply, float lr) 
   cudaStream_t st = net->stream;
   cudaError_t e;
   float *loss = net->loss.p;
-  e = cudaMemsetAsync(loss, 0, sizeof(float), st);
-  if (e != cudaSuccess) return cuda_fail(e, "surrogate");
-  head_y_kernel<<<B / 8, 256, 0, st>>>(net->A[2].p, net->w4.p, net->b4.p, B, net->H, d_target,
-                                        net->y.p, net->dy.p, loss);
-  head_dz_kernel<<<dim3(B / 32, net->H / 64), 256, 0, st>>>(net->Z[2].p, net->w4.p, net->dy.p, B,
-                                                            net->H, net->dZ[2].p, net->dZT[2].p);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "surrogate head");
+  // the loss sum was zeroed by the input packing of this step
+  e = launch_pdl(head_y_kernel, dim3(B / 8), dim3(256), 0, st, (const __nv_bfloat16 *)net->A[2].p,
+                 (const float *)net->w4.p, (const float *)net->b4.p, B, net->H, d_target,
+                 net->y.p, net->dy.p, loss);
+  if (e == cudaSuccess)
+    e = launch_pdl(head_dz_kernel, dim3(B / 32, net->H / 64), dim3(256), 0, st,
+                   (const __nv_bfloat16 *)net->Z[2].p, (const float *)net->w4.p,
+                   (const float *)net->dy.p, B, net->H, net->dZ[2].p, net->dZT[2].p);
+  if (e != cudaSuccess) return cuda_fail(e, "surrogate head");
   ++net->step;
   const float bc1 = 1.0f - std::pow(net->beta1, static_cast<float>(net->step));
   const float bc2 = 1.0f - std::pow(net->beta2, static_cast<float>(net->step));
@@ -746,11 +791,11 @@ int backward(emt6_mlp *net, int B, const float *d_target, bool apply, float lr) 
       ep.c_out = net->work.p;
       e = launch_gemm<EPI_STORE_F32>(net->mdZT[l], bmap, net->H, N, B, ep, st, splits);
       if (e == cudaSuccess) {
-        adam_reduce_kernel<<<dim3(N / 32, net->H / 32), 1024, 0, st>>>(
-            net->work.p, splits, net->H, N, net->w[l].p, net->m[l].p, net->v[l].p, net->wb[l].p,
-            net->wbt[l].p, apply ? nullptr : net->gradw[l].p, lr, net->beta1, net->beta2,
-            net->eps, bc1, bc2);
-        e = cudaGetLastError();
+        e = launch_pdl(adam_reduce_kernel, dim3(N / 32, net->H / 32), dim3(1024), 0, st,
+                       (const float *)net->work.p, splits, net->H, N, net->w[l].p, net->m[l].p,
+                       net->v[l].p, net->wb[l].p, net->wbt[l].p,
+                       apply ? nullptr : net->gradw[l].p, lr, net->beta1, net->beta2, net->eps,
+                       bc1, bc2);
       }
     } else if (apply) {
       EpiArgs ep = base_args(net, net->H, N);
@@ -782,18 +827,17 @@ int backward(emt6_mlp *net, int B, const float *d_target, bool apply, float lr) 
   vp[4] = {net->b4.p, net->mb4.p, net->vb4.p, nullptr, net->dy.p,
            apply ? nullptr : net->gradv[4].p, 1};
   const int warps = 4 * net->H + 1;
-  vec_adam_kernel<<<(warps * 32 + 255) / 256, 256, 0, st>>>(vp[0], vp[1], vp[2], vp[3], vp[4], B,
-                                                             lr, net->beta1, net->beta2, net->eps,
-                                                             bc1, bc2, apply ? 1 : 0);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "surrogate vector Adam");
+  e = launch_pdl(vec_adam_kernel, dim3((warps * 32 + 255) / 256), dim3(256), 0, st, vp[0], vp[1],
+                 vp[2], vp[3], vp[4], B, lr, net->beta1, net->beta2, net->eps, bc1, bc2,
+                 apply ? 1 : 0);
+  if (e != cudaSuccess) return cuda_fail(e, "surrogate vector Adam");
   if (!apply) --net->step;
   return EMT6_OK;
 }
 
 int pack(emt6_mlp *net, const float *d_x, int B) {
-  pack_input_kernel<<<B / 32, 256, 0, net->stream>>>(d_x, B, net->in, net->in_pad, net->X.p,
-                                                      net->XT.p);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_pdl(pack_input_kernel, dim3(B / 32), dim3(256), 0, net->stream, d_x, B,
+                             net->in, net->in_pad, net->X.p, net->XT.p, net->loss.p);
   return e == cudaSuccess ? EMT6_OK : cuda_fail(e, "surrogate input");
 }
 
@@ -944,9 +988,10 @@ int emt6_mlp_predict(emt6_mlp *net, const float *d_x, int B, float *d_y) {
   if (rc == EMT6_OK) rc = pack(net, d_x, B);
   if (rc == EMT6_OK) rc = forward_hidden(net, B);
   if (rc != EMT6_OK) return rc;
-  head_y_kernel<<<B / 8, 256, 0, net->stream>>>(net->A[2].p, net->w4.p, net->b4.p, B, net->H,
-                                                  nullptr, d_y, nullptr, nullptr);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_pdl(head_y_kernel, dim3(B / 8), dim3(256), 0, net->stream,
+                             (const __nv_bfloat16 *)net->A[2].p, (const float *)net->w4.p,
+                             (const float *)net->b4.p, B, net->H, (const float *)nullptr, d_y,
+                             (float *)nullptr, (float *)nullptr);
   return e == cudaSuccess ? EMT6_OK : cuda_fail(e, "emt6_mlp_predict");
 }
 
