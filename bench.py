@@ -628,7 +628,7 @@ def main():
                     help="surrogate: simulated steps per simulation")
     ap.add_argument("--train-pairs", type=int, default=96_000)
     ap.add_argument("--train-reps", type=int, default=1)
-    ap.add_argument("--epochs", type=int, default=60)
+    ap.add_argument("--epochs", type=int, default=200)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--population", type=int, default=10_000)
     ap.add_argument("--elite-frac", type=float, default=0.05)

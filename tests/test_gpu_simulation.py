@@ -192,3 +192,27 @@ def test_summary_and_timelapse_match_oracle_states(params, oracle):
             want += [(s["mode"][occ] == m).sum() for m in range(4)]
             want += [(s["phase"][occ] == ph).sum() for ph in range(5)]
             assert np.array_equal(rec[k, i], np.array(want, np.float32)), (k, i)
+
+
+def test_autotuner_picks_a_schedule_that_changes_nothing_but_time(params):
+    """The launch autotuner times (schedule mode, steps per launch) candidates
+    on a sample and returns the fastest; any schedule it can pick gives the
+    same lattices as the default one."""
+    from emt6ro import autotune, workloads as wl
+    from emt6ro.batch import Batch
+    tumors = [wl.disc_tumor(params, r, seed=80 + r) for r in (5, 9, 13)]
+    protocols = [[(60, 2.0)], [(0, 1.0), (120, 1.0)]]
+    st = np.arange(24, dtype=np.int32) % 3
+    sp = np.arange(24, dtype=np.int32) % 2
+    hz = np.where(np.arange(24) % 4 == 0, 150, 300).astype(np.uint32)
+    mode, chunk, table = autotune.tune(params, tumors, protocols, st, sp, hz, sample=12,
+                                       trial_steps=64, warm_steps=16, chunks=(32, 64),
+                                       modes=(0, 1, 2, 3))
+    assert len(table) == 8 and (mode, chunk) in [(m, c) for m, c, _ in table]
+    ref = Batch(params, tumors, protocols, st, sp, sim_horizon=hz, seed=5)
+    ref.run(300)
+    tuned = Batch(params, tumors, protocols, st, sp, sim_horizon=hz, seed=5)
+    tuned.set_schedule(mode, chunk)
+    tuned.run(300)
+    for i in range(24):
+        assert tuned.state(i).sites.tobytes() == ref.state(i).sites.tobytes()
