@@ -256,8 +256,6 @@ def run_ours(args, rank, world, dist):
     import torch
     from emt6ro import _native as N
     from emt6ro.batch import Batch
-    from emt6ro import simulation as sim
-    from emt6ro import workloads as wl
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)

@@ -1,19 +1,23 @@
 // emt6_kernels.cu -- sm_103a kernels of the EMT6-Ro batched simulation step.
 //
-// One CTA (192 threads) owns one simulation for a whole launch of N steps:
-// the three substrate fields (3 x 53 x 53 FP32), the site-state bytes and the
-// occupied list live in shared memory for the launch; per-site cell records
-// (48 B) stay in global memory, where the few hundred live cells of each
-// resident simulation stay L2-resident.  Per step (reference cadence,
-// src/emt6ro/simulation/simulation.cu:153-166):
+// One CTA owns one simulation for a whole launch of N steps: the three
+// substrate fields (3 x 53 x 53 FP32), the site-state bytes and the occupied
+// list live in shared memory for the launch; per-site cell records (48 B)
+// stay in global memory, where the few hundred live cells of each resident
+// simulation stay L2-resident.  Two kernels: run_kernel<false> (192 threads,
+// 4 CTAs/SM) for regions up to 32 x 32 (33 x 33 with a fixed ring), and
+// run_kernel<true> (384 threads, 2 CTAs/SM) for wider regions.  Per step
+// (reference cadence, src/emt6ro/simulation/simulation.cu:153-166):
 //   t % 128 == 0  rebuild the occupied list        (simulation.cu:41-64)
 //   t % 32  == 0  ROI + circular fixed-value mask   (diffusion.cu:65-100)
 //   diffusion: 23 substeps over free sites + 1 over the ROI (diffusion.cu:135-191).
-//     Each field is held in registers by a pair of warps (rows split in two
-//     halves; lane = column, or two columns for ROIs wider than 31); the
-//     horizontal neighbours come from warp shuffles, vertical ones from the
-//     same thread's registers, and the two halves swap one boundary row per
-//     substep through shared memory under a 64-thread named barrier.
+//     Each field is held in registers, two columns per lane: in the narrow
+//     kernel by a pair of warps whose half-warps hold four bands of rows
+//     (diffuse_half), in the wide kernel by four warps of one band each
+//     (diffuse_part).  Horizontal neighbours come from warp shuffles,
+//     vertical ones from the same thread's registers; bands swap one
+//     boundary row per substep (a shuffle across half-warps, shared memory
+//     between warps under 64- or 128-thread named barriers).
 //   cell update: 8-neighbour vacancy snapshot, Site::step per list entry,
 //     at most one division per simulation (simulation.cu:66-110).
 // Randomness is Philox keyed by (step, simulation, site, occurrence), so the
@@ -271,9 +275,9 @@ __device__ void narrow_mapping(const uint64_t *colmask, Misc *m) {
 }
 
 // ---------------------------------------------------------------------------
-// diffusion of one field by one warp of NP (part k = region rows
-// [k*RH, (k+1)*RH) of the (h+2) x (w+2) region; lane = column, or columns
-// 2*lane, 2*lane+1 when WIDE).
+// diffusion of one field by one warp of NP = 4 (wide kernel; part k = region
+// rows [k*RH, (k+1)*RH) of the (h+2) x (w+2) region; lane = column for
+// regions up to 31 columns, columns 2*lane, 2*lane+1 when WIDE).
 // With H = x_left + x_right and G = b*x + d*H per site (fmaf(d, H, b*x)):
 //   x' = a*x + b*(H + x_up + x_down) + d*(H_up + H_down)
 //      = fmaf(a, x, fmaf(b, H, G_up + G_down))

@@ -12,8 +12,6 @@ from __future__ import annotations
 
 import time
 
-import numpy as np
-
 from .. import simulation as sim
 from ..surrogate import prescreen
 

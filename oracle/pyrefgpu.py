@@ -38,7 +38,7 @@ def _load():
             from oracle import build
             build.build_ref_gpu_driver()
         L = ctypes.CDLL(str(LIB))
-        vp, i32, u32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64
+        vp, u32, i64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int64
         L.refgpu_create.restype = vp
         L.refgpu_create.argtypes = [ctypes.c_char_p, vp, vp, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, vp, vp, vp, ctypes.c_int, u32, u32, u32, i64,

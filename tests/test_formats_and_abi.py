@@ -3,7 +3,6 @@ CPU: the library's host-side loaders are compared with the reference's own
 loaders (golden fixtures from tests/golden/make_golden.py), every symbol
 declared in include/*.h is exported and bound, and errors come
 back as exceptions with the reference's messages."""
-import ctypes
 import json
 import re
 from pathlib import Path

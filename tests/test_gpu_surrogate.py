@@ -3,8 +3,6 @@ float64 products of the same BF16 inputs, the forward pass, gradients and one
 Adam step against the CPU oracle (oracle/mlp_oracle.py), and training on
 simulator output: held-out accuracy and what pre-screening with the trained
 network gains over pre-screening without it (a random subset)."""
-import ctypes
-
 import numpy as np
 import pytest
 
@@ -96,8 +94,7 @@ def test_split_k_weight_gradients_agree():
     kernel, and one Adam step through the split path (reduce kernel) agrees
     with the fused Adam epilogue."""
     from emt6ro import _native as Nat
-    from oracle import mlp_oracle as mo
-    net, params = _net(7)
+    net, _ = _net(7)
     rng = np.random.default_rng(8)
     x = rng.normal(size=(1024, 100)).astype(np.float32)
     t = rng.normal(size=1024).astype(np.float32)

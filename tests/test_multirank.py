@@ -4,7 +4,6 @@ the step time is the max over ranks."""
 import os
 import socket
 
-import pytest
 
 
 def _free_port():

@@ -6,7 +6,6 @@ import ctypes
 import math
 
 import numpy as np
-import pytest
 
 from conftest import GOLDEN
 
