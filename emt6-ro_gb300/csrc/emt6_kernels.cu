@@ -798,7 +798,12 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
       __syncthreads();
 
       // ---- cell update (simulation.cu:84-96) ----
-      bool any_ready = false;
+      // may_divide: some cell is ready and may find a vacant neighbour.  A
+      // ready cell whose 8 neighbours were all taken at the vacancy snapshot
+      // can only find one if a neighbour dies in this step (divisions fill
+      // sites only after the arbitration), so the arbitration runs only when
+      // a ready cell had a vacant neighbour or some cell died.
+      bool may_divide = false;
       const float dose =
           (t < p.length && t % p.res == 0 && t / p.res < p.bins) ? doses[t / p.res] : 0.f;
       {
@@ -826,10 +831,11 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
             continue;
           }
           if (sv & kStMulti) continue;  // stepped in list order below
-          const bool ready = step_site(p, fld, st, cells, s, c, aux[e], dose, t, (uint32_t)sim,
-                                       0, a.epoch, m);
+          const uint32_t vac = aux[e];
+          const bool ready = step_site(p, fld, st, cells, s, c, vac, dose, t, (uint32_t)sim, 0,
+                                       a.epoch, m);
           aux[e] = ready ? 0x80 : 0;
-          any_ready |= ready;
+          may_divide |= (ready && vac != 0) || (st[s] & kStMask) == kVacant;
         }
       }
       if (m->has_multi && wid == 0) {
@@ -848,14 +854,14 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
               const int s = list[ee];
               uint8_t res = 0;
               if ((st[s] & kStMask) == kOccupied) {
-                const bool ready = step_site(p, fld, st, cells, s, load_cell(cells + 3 * s),
-                                             aux[ee] & 15u, dose, t, (uint32_t)sim, occ,
-                                             a.epoch, m);
+                const uint32_t vac = aux[ee] & 15u;
+                const bool ready = step_site(p, fld, st, cells, s, load_cell(cells + 3 * s), vac,
+                                             dose, t, (uint32_t)sim, occ, a.epoch, m);
                 if (ready) {
                   if (occ > 127) atomicOr(a.err, 4u);
                   res = (uint8_t)(0x80 | (occ & 0x7f));
-                  any_ready = true;
                 }
+                may_divide |= (ready && vac != 0) || (st[s] & kStMask) == kVacant;
               }
               aux[ee] = res;
             }
@@ -863,8 +869,8 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
           }
         }
       }
-      // most steps have no cell ready to divide: skip the arbitration then
-      if (!__syncthreads_or(any_ready)) continue;
+      // most steps have no cell that may divide: skip the arbitration then
+      if (!__syncthreads_or(may_divide)) continue;
 
       // ---- division arbitration: lowest list index with a vacant target ----
       int best = 0x7fffffff, best_target = -1;
