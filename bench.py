@@ -422,8 +422,9 @@ def run_surrogate(args):
        --train-reps simulations of --horizon steps (default 144,000 = 10
        days).  5% of the pairs are held out for the reported error, 5% of the
        rest select the best epoch.
-    2. Training: Adam, batch 4096, on the GPU by the library's tcgen05 BF16
-       kernels; the training step is also timed alone with CUDA events.
+    2. Training: an ensemble of --ensemble surrogates (Adam, batch 4096, on
+       the GPU by the library's tcgen05 BF16 kernels); the training step is
+       also timed alone with CUDA events.
     3. GA generation: --population protocols x 20 tumours scored by the
        surrogate; the best --elite-frac re-simulated with --elite-sims
        simulations each (20 tumours x runs).  Plain scoring would simulate
@@ -448,16 +449,20 @@ def run_surrogate(args):
     data_s = time.perf_counter() - t0
     x = S.features(protocols, tumors, pp, pt)
     train = np.random.default_rng(2026).random(P) >= 0.05
-    # 2. training
-    net = S.Surrogate(max_batch=4096, seed=0)
+    # 2. training: an ensemble of --ensemble members
+    ens = S.SurrogateEnsemble(k=args.ensemble, max_batch=4096, seed=0)
     t0 = time.perf_counter()
-    net.fit(x[train], y[train], epochs=args.epochs, lr=args.lr, batch=4096, val_frac=0.05)
+    ens.fit(x[train], y[train], epochs=args.epochs, lr=args.lr, batch=4096, val_frac=0.05)
     fit_s = time.perf_counter() - t0
-    pred_held = net.predict(x[~train])
+    net = ens.nets[0]
+    pred_held = ens.predict(x[~train])
+    pred_single = net.predict(x[~train])
     err = pred_held - y[~train]
     held = {"rmse_cells": float(np.sqrt(np.mean(err ** 2))),
             "rmse_over_mean": float(np.sqrt(np.mean(err ** 2)) / np.mean(y[~train])),
             "r2": float(1 - np.mean(err ** 2) / np.var(y[~train])),
+            "r2_single_member": float(1 - np.mean((pred_single - y[~train]) ** 2) /
+                                      np.var(y[~train])),
             "pairs": int((~train).sum())}
     # training-step throughput on one resident batch (CUDA events on the
     # surrogate's stream)
@@ -487,7 +492,7 @@ def run_surrogate(args):
     runs = max(1, args.elite_sims // T)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    elite, pred = S.prescreen(net, pop, tumors, keep)
+    elite, pred = S.prescreen(ens, pop, tumors, keep)
     score_s = time.perf_counter() - t0
     st = np.tile(np.repeat(np.arange(T, dtype=np.int32), runs), keep)
     sp = np.repeat(np.arange(keep, dtype=np.int32), T * runs)
@@ -518,7 +523,8 @@ def run_surrogate(args):
                                f"tumours, top {keep} re-simulated with {T * runs} simulations "
                                f"each, {horizon}-step horizon",
                    "train_pairs": int(train.sum()), "train_reps": args.train_reps,
-                   "best_epoch": int(np.argmin(net.val_history)) if net.val_history else None,
+                   "ensemble": args.ensemble,
+                   "best_epochs": [int(np.argmin(m.val_history)) for m in ens.nets],
                    "epochs": args.epochs, "batch": 4096},
         "plain_protocols_per_s": plain_rate, "speedup_vs_plain": screened_rate / plain_rate,
         "elites": {"spearman": _spearman(pe, sim_mean),
@@ -626,8 +632,10 @@ def main():
                     help="surrogate: simulated steps per simulation")
     ap.add_argument("--train-pairs", type=int, default=96_000)
     ap.add_argument("--train-reps", type=int, default=1)
-    ap.add_argument("--epochs", type=int, default=200)
+    ap.add_argument("--epochs", type=int, default=100)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--ensemble", type=int, default=5,
+                    help="surrogate: members averaged for pre-screening")
     ap.add_argument("--population", type=int, default=10_000)
     ap.add_argument("--elite-frac", type=float, default=0.05)
     ap.add_argument("--elite-sims", type=int, default=100)

@@ -228,3 +228,13 @@ def test_screened_model_simulates_only_the_elites(params, trained):
     # the elites' simulated fitness is what the plain model gives them
     plain = EMT6RoModel(params, tumors, 3, 2, num_steps=28_800, seed=3)
     assert np.allclose(plain.predict([protocols[i] for i in elite]), fit[elite])
+
+
+def test_ensemble_averages_its_members(dataset_48h):
+    from emt6ro.surrogate import SurrogateEnsemble
+    x, y = dataset_48h
+    ens = SurrogateEnsemble(k=2, max_batch=512, seed=9)
+    ens.fit(x[:2560], y[:2560], epochs=20, lr=1e-3, batch=512)
+    members = [net.predict(x[2560:]) for net in ens.nets]
+    assert not np.allclose(members[0], members[1])           # independent members
+    assert np.allclose(ens.predict(x[2560:]), np.mean(members, axis=0))
