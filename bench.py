@@ -62,6 +62,17 @@ def shard_range(total: int, rank: int, world: int):
     return lo, lo + base + (1 if rank < extra else 0)
 
 
+def large_batch(n: int = 4864):
+    """Simulations of the ragged-batch tumours with disc radius >= 15: their
+    regions outgrow the narrow kernel, so the wide kernel does the work."""
+    from emt6ro import workloads as wl
+    params = wl.default_parameters()
+    tumors, protocols, st, sp, _ = wl.ragged_batch(params, 30_000)
+    radii = np.array([np.sqrt((t.sites["state"] == 1).sum() / np.pi) for t in tumors])
+    keep = np.nonzero(radii[st] >= 14.5)[0][:n]
+    return params, tumors, protocols, st[keep], sp[keep]
+
+
 def ga_batch(n_reps: int = 20):
     from emt6ro import workloads as wl
     params = wl.default_parameters()
@@ -259,7 +270,7 @@ def run_ours(args, rank, world, dist):
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    params, tumors, protocols, st, sp = ga_batch()
+    params, tumors, protocols, st, sp = large_batch() if args.workload == "large" else ga_batch()
     if args.sims:
         # a stratified subset of the batch (profiling captures of a small case)
         keep = np.unique(np.linspace(0, len(st) - 1, args.sims).astype(np.int64))
@@ -305,7 +316,7 @@ def run_ours(args, rank, world, dist):
     bins = (144_000 + 299) // 300
     e2e_value = None
     h2d = d2h = 0
-    if not args.no_e2e and not args.sims:
+    if not args.no_e2e and not args.sims and args.workload == "ga":
         e2e_value, h2d, d2h = _e2e(args, params, tumors, protocols, dev, seed, world, dist, bins)
 
     # ---- roofline of the dominant kernel -------------------------------------
@@ -315,7 +326,7 @@ def run_ours(args, rank, world, dist):
     achieved = diffused / args.steps * FLOP_PER_SITE_SUBSTEP / (kernel_ms * 1e-3) / 1e12
     profiles = ROOT / "profiles" / "traffic.json"
     traffic = None
-    if profiles.exists():
+    if profiles.exists() and args.workload == "ga":
         try:
             cap = json.loads(profiles.read_text())["captured"]
             # per launch each simulation's state is read and written once
@@ -342,10 +353,14 @@ def run_ours(args, rank, world, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded disc tumours and protocols, default parameters)",
-        "config": {"workload": "GA batch: 20 tumours x 100 protocols x 20 runs = 40,000 "
-                               "simulations per GPU, 53x53 lattice, 6-s steps",
+        "config": {"workload": ("GA batch: 20 tumours x 100 protocols x 20 runs = 40,000 "
+                                "simulations per GPU, 53x53 lattice, 6-s steps")
+                               if args.workload == "ga" else
+                               (f"large tumours: {B} simulations of the ragged batch's disc "
+                                "radius >= 15 tumours (wide kernel), 53x53 lattice, 6-s steps"),
                    "sim_steps_per_step": args.sim_steps, "simulations_per_gpu": B,
-                   "l2": "state 7 GB per GPU >> 129 MB L2; no flush needed",
+                   "l2": f"state {B * 176 / 1e6:.1f} MB per GPU (> 129 MB L2); no flush "
+                         "needed",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
@@ -623,9 +638,10 @@ def main():
                          "profiling case; implies --no-e2e)")
     ap.add_argument("--no-ref-cuda", action="store_true",
                     help="--impl reference: skip timing the reference's CUDA kernels")
-    ap.add_argument("--workload", choices=["ga", "ragged", "surrogate", "surrogate-train"],
+    ap.add_argument("--workload", choices=["ga", "large", "ragged", "surrogate", "surrogate-train"],
                     default="ga",
                     help="ga: 40,000-simulation GA batch (default, the headline); "
+                         "large: 4,864 simulations of radius >= 15 tumours (wide kernel); "
                          "ragged: 30,000 simulations with mixed sizes and horizons; "
                          "surrogate: surrogate training + a screened GA generation")
     ap.add_argument("--horizon", type=int, default=144_000,
@@ -664,7 +680,8 @@ def main():
     else:
         line = run_ours(args, rank, world, dist)
         if rank == 0 and not args.no_cpu_baseline:
-            params, tumors, protocols, st, sp = ga_batch()
+            params, tumors, protocols, st, sp = (large_batch() if args.workload == "large"
+                                                 else ga_batch())
             rates, threads, n = cpu_sample(params, tumors, protocols, st, sp, 2, 1,
                                            args.sim_steps)
             line["cpu_baseline"] = {
