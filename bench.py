@@ -359,7 +359,7 @@ def run_ours(args, rank, world, dist):
                                (f"large tumours: {B} simulations of the ragged batch's disc "
                                 "radius >= 15 tumours (wide kernel), 53x53 lattice, 6-s steps"),
                    "sim_steps_per_step": args.sim_steps, "simulations_per_gpu": B,
-                   "l2": f"state {B * 176 / 1e6:.1f} MB per GPU (> 129 MB L2); no flush "
+                   "l2": f"state {B * 176e3 / 1e9:.1f} GB per GPU (> 129 MB L2); no flush "
                          "needed",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
@@ -687,7 +687,7 @@ def main():
             line["cpu_baseline"] = {
                 "value": statistics.median(rates), "unit": METRIC, "cores": threads,
                 "kind": "port",
-                "sample": f"{n} of the 40,000 simulations x {args.sim_steps} steps, "
+                "sample": f"{n} of the {len(st):,} simulations x {args.sim_steps} steps, "
                           "oracle/emt6_oracle.c restatement of the reference CPU path"}
     if rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
