@@ -621,6 +621,7 @@ __device__ __forceinline__ bool step_site(const KParams &p, float *fld, uint8_t 
                                           float dose, uint32_t t, uint32_t sim, uint32_t occ,
                                           uint32_t epoch, Misc *m) {
   const int HW = p.HW;
+  const uint32_t mp0 = c.mode | (c.phase << 8);
   float l0 = fld[s], l1 = fld[HW + s], l2 = fld[2 * HW + s];
   if (!update_state(c, l0, l1, l2, p, vac)) {
     st[s] = (st[s] & ~kStMask) | kVacant;
@@ -658,7 +659,11 @@ __device__ __forceinline__ bool step_site(const KParams &p, float *fld, uint8_t 
       c.delay = 0.f;
     }
   }
-  store_cell(cells + 3 * s, c);
+  // the cycle times (t0..t4) never change here: store the clocks and, when
+  // they changed, mode and phase (same memory contents as a full store)
+  cells[3 * s] = make_float4(c.prolif, c.tir, c.irr, c.delay);
+  const uint32_t mp = c.mode | (c.phase << 8);
+  if (mp != mp0) reinterpret_cast<float2 *>(cells + 3 * s + 2)[0] = make_float2(c.t4, __uint_as_float(mp));
   if (dead) {
     st[s] = (st[s] & ~kStMask) | kVacant;
     return false;
