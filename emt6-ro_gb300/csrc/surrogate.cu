@@ -851,6 +851,20 @@ int refresh_bf16(emt6_mlp *net) {
   return EMT6_OK;
 }
 
+// The 8 FP32 parameter arrays in the C ABI's order and their element counts.
+void param_arrays(emt6_mlp *net, float *dev[8], size_t cnt[8]) {
+  for (int l = 0; l < 3; ++l) {
+    dev[2 * l] = net->w[l].p;
+    cnt[2 * l] = static_cast<size_t>(rows_of(l)) * cols_of(l);
+    dev[2 * l + 1] = net->b[l].p;
+    cnt[2 * l + 1] = net->H;
+  }
+  dev[6] = net->w4.p;
+  cnt[6] = net->H;
+  dev[7] = net->b4.p;
+  cnt[7] = 1;
+}
+
 // Batch-size-dependent maps are rebuilt when B changes.
 int ensure_maps(emt6_mlp *net, int B) {
   if (net->cur_b == B) return EMT6_OK;
@@ -900,7 +914,8 @@ int emt6_mlp_create(int max_batch, uint64_t seed, int device, emt6_mlp **out) {
   // He-style initialisation from a seeded generator; biases and moments zero
   std::mt19937_64 rng(seed);
   std::vector<float> host;
-  for (int l = 0; l < 4; ++l) {
+  e = cudaSuccess;
+  for (int l = 0; l < 4 && e == cudaSuccess; ++l) {
     const int rows = l < 3 ? rows_of(l) : 1, cols = l < 3 ? cols_of(l) : H;
     const int fan_in = l == 0 ? net->in : H;
     std::normal_distribution<float> nd(0.0f, std::sqrt(2.0f / static_cast<float>(fan_in)));
@@ -909,22 +924,23 @@ int emt6_mlp_create(int max_batch, uint64_t seed, int device, emt6_mlp **out) {
       for (int c = 0; c < cols; ++c)
         if (l != 0 || c < net->in) host[static_cast<size_t>(r) * cols + c] = nd(rng);
     float *dst = l < 3 ? net->w[l].p : net->w4.p;
-    cudaMemcpy(dst, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(dst, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice);
   }
-  for (int l = 0; l < 3; ++l) {
-    const size_t n = static_cast<size_t>(rows_of(l)) * cols_of(l);
-    cudaMemset(net->m[l].p, 0, n * 4);
-    cudaMemset(net->v[l].p, 0, n * 4);
-    cudaMemset(net->b[l].p, 0, H * 4);
-    cudaMemset(net->bm[l].p, 0, H * 4);
-    cudaMemset(net->bv[l].p, 0, H * 4);
+  float *zero[] = {net->m[0].p, net->v[0].p, net->m[1].p, net->v[1].p, net->m[2].p, net->v[2].p,
+                   net->b[0].p, net->bm[0].p, net->bv[0].p, net->b[1].p, net->bm[1].p,
+                   net->bv[1].p, net->b[2].p, net->bm[2].p, net->bv[2].p, net->m4.p, net->v4.p,
+                   net->b4.p, net->mb4.p, net->vb4.p};
+  const size_t zn[] = {net->m[0].n, net->v[0].n, net->m[1].n, net->v[1].n, net->m[2].n,
+                       net->v[2].n, net->b[0].n, net->bm[0].n, net->bv[0].n, net->b[1].n,
+                       net->bm[1].n, net->bv[1].n, net->b[2].n, net->bm[2].n, net->bv[2].n,
+                       net->m4.n, net->v4.n, net->b4.n, net->mb4.n, net->vb4.n};
+  for (size_t i = 0; i < sizeof(zero) / sizeof(zero[0]) && e == cudaSuccess; ++i)
+    e = cudaMemset(zero[i], 0, zn[i] * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(net->err.p, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    emt6_mlp_destroy(net);
+    return cuda_fail(e, "emt6_mlp_create");
   }
-  cudaMemset(net->m4.p, 0, H * 4);
-  cudaMemset(net->v4.p, 0, H * 4);
-  cudaMemset(net->b4.p, 0, 4);
-  cudaMemset(net->mb4.p, 0, 4);
-  cudaMemset(net->vb4.p, 0, 4);
-  cudaMemset(net->err.p, 0, 4);
   int rc = refresh_bf16(net);
   if (rc == EMT6_OK) {
     e = cudaStreamSynchronize(net->stream);
@@ -951,13 +967,12 @@ void *emt6_mlp_stream(emt6_mlp *net) { return net ? net->stream : nullptr; }
 int emt6_mlp_set_params(emt6_mlp *net, const float *const *host) {
   if (!net || !host) return fail("emt6_mlp_set_params: null argument", EMT6_ERR_INVALID);
   cudaSetDevice(net->device);
-  for (int l = 0; l < 3; ++l) {
-    const size_t n = static_cast<size_t>(rows_of(l)) * cols_of(l);
-    cudaMemcpy(net->w[l].p, host[2 * l], n * 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(net->b[l].p, host[2 * l + 1], net->H * 4, cudaMemcpyHostToDevice);
-  }
-  cudaMemcpy(net->w4.p, host[6], net->H * 4, cudaMemcpyHostToDevice);
-  cudaError_t e = cudaMemcpy(net->b4.p, host[7], 4, cudaMemcpyHostToDevice);
+  float *dev[8];
+  size_t cnt[8];
+  param_arrays(net, dev, cnt);
+  cudaError_t e = cudaStreamSynchronize(net->stream);
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i)
+    e = cudaMemcpy(dev[i], host[i], cnt[i] * sizeof(float), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "emt6_mlp_set_params");
   int rc = refresh_bf16(net);
   if (rc != EMT6_OK) return rc;
@@ -968,15 +983,12 @@ int emt6_mlp_set_params(emt6_mlp *net, const float *const *host) {
 int emt6_mlp_get_params(emt6_mlp *net, float *const *host) {
   if (!net || !host) return fail("emt6_mlp_get_params: null argument", EMT6_ERR_INVALID);
   cudaSetDevice(net->device);
+  float *dev[8];
+  size_t cnt[8];
+  param_arrays(net, dev, cnt);
   cudaError_t e = cudaStreamSynchronize(net->stream);
-  if (e != cudaSuccess) return cuda_fail(e, "emt6_mlp_get_params");
-  for (int l = 0; l < 3; ++l) {
-    const size_t n = static_cast<size_t>(rows_of(l)) * cols_of(l);
-    cudaMemcpy(host[2 * l], net->w[l].p, n * 4, cudaMemcpyDeviceToHost);
-    cudaMemcpy(host[2 * l + 1], net->b[l].p, net->H * 4, cudaMemcpyDeviceToHost);
-  }
-  cudaMemcpy(host[6], net->w4.p, net->H * 4, cudaMemcpyDeviceToHost);
-  e = cudaMemcpy(host[7], net->b4.p, 4, cudaMemcpyDeviceToHost);
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i)
+    e = cudaMemcpy(host[i], dev[i], cnt[i] * sizeof(float), cudaMemcpyDeviceToHost);
   return e == cudaSuccess ? EMT6_OK : cuda_fail(e, "emt6_mlp_get_params");
 }
 
@@ -1028,13 +1040,14 @@ int emt6_mlp_gradients(emt6_mlp *net, const float *d_x, const float *d_target, i
   if (rc == EMT6_OK) rc = backward(net, B, d_target, false, 0.0f);
   if (rc != EMT6_OK) return rc;
   if ((rc = read_err(net)) != EMT6_OK) return rc;
-  for (int l = 0; l < 3; ++l) {
-    const size_t n = static_cast<size_t>(rows_of(l)) * cols_of(l);
-    cudaMemcpy(host_grads[2 * l], net->gradw[l].p, n * 4, cudaMemcpyDeviceToHost);
-    cudaMemcpy(host_grads[2 * l + 1], net->gradv[l].p, net->H * 4, cudaMemcpyDeviceToHost);
-  }
-  cudaMemcpy(host_grads[6], net->gradv[3].p, net->H * 4, cudaMemcpyDeviceToHost);
-  cudaError_t e = cudaMemcpy(host_grads[7], net->gradv[4].p, 4, cudaMemcpyDeviceToHost);
+  const float *grad[8] = {net->gradw[0].p, net->gradv[0].p, net->gradw[1].p, net->gradv[1].p,
+                          net->gradw[2].p, net->gradv[2].p, net->gradv[3].p, net->gradv[4].p};
+  float *dev[8];
+  size_t cnt[8];
+  param_arrays(net, dev, cnt);
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i)
+    e = cudaMemcpy(host_grads[i], grad[i], cnt[i] * sizeof(float), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && h_loss) {
     float s = 0.0f;
     e = cudaMemcpy(&s, net->loss.p, 4, cudaMemcpyDeviceToHost);
