@@ -7,8 +7,8 @@ G1, mean oxygen over occupied sites) to the mean final living-cell count of
 that (protocol, tumour) pair.  It is trained only on simulator output, on the
 GPU, by the library's own BF16 tensor-core kernels (include/emt6ro_surrogate.h;
 forward, backward and Adam); a GA scores a whole population with it and
-re-simulates only the best fraction (`ScreenedModel`), so full simulation stays
-the judge of every protocol it keeps.
+re-simulates only the best fraction (`ScreenedModel`), so full simulation still
+decides the fitness of every protocol it keeps.
 
 The reference has no surrogate: its GA scores every protocol by simulation
 (python/emt6ro/ga_model/model.py:33-54).

@@ -5,14 +5,13 @@ declared in include/*.h is exported and bound, and errors come
 back as exceptions with the reference's messages."""
 import json
 import re
-from pathlib import Path
 
 import numpy as np
 import pytest
 
 from conftest import GOLDEN, ROOT
 
-REF = Path("/root/reference")
+from oracle.build import REFERENCE_ROOT as REF  # noqa: E402  (the reference checkout, if present)
 
 
 def _N():
