@@ -1,4 +1,4 @@
-// emt6_host.cpp -- host engine and C ABI of the GB300 EMT6-Ro simulator.
+// emt6_host.cu -- host engine and C ABI of the GB300 EMT6-Ro simulator.
 //
 // Replaces, on the host side, the reference's Simulation class
 // (src/emt6ro/simulation/simulation.{h,cu}), its pybind11 Experiment
