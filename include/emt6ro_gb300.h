@@ -77,7 +77,7 @@ int emt6_version(void);
 /* Replaces Parameters::loadFromJSONFile (src/emt6ro/parameters/parameters.cc:66-80). */
 int emt6_load_parameters(const char *path, emt6_params *out);
 /* Replaces loadFromFile (src/emt6ro/state/state.cc:9-53).  Writes (H+2)*(W+2)
- * sites with the MOCKED border ring at the external levels; *height/*width are
+ * sites with the MOCKED border ring at the external levels; *height and *width are
  * the full dims.  Fails with EMT6_ERR_LIMIT if more than cap sites. */
 int emt6_load_state(const char *path, const emt6_params *p, emt6_site *out, int32_t cap,
                     int32_t *height, int32_t *width);
