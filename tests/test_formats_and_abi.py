@@ -148,3 +148,21 @@ def test_experiment_result_shape_api():
                                         "gpu_id", "simulation_steps", "protocol_resolution"]
     assert sig.parameters["simulation_steps"].default == 144000
     assert sig.parameters["protocol_resolution"].default == 300
+
+
+def test_integration_c_example_compiles(tmp_path):
+    """The C example in INTEGRATION.md compiles against include/ without warnings."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    doc = (ROOT / "INTEGRATION.md").read_text()
+    a = doc.index("```c\n") + 5
+    code = doc[a:doc.index("```", a)]
+    code = code.replace('#include "emt6ro_gb300.h"', '#include "emt6ro_gb300.h"\nint main(void) {')
+    src = tmp_path / "example.c"
+    src.write_text("#include <stdio.h>\n#include <stdlib.h>\n" + code + "return 0; }\n")
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
+                        "-c", str(src), "-o", str(tmp_path / "example.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
