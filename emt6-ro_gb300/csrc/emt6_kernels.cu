@@ -13,7 +13,9 @@
 //   diffusion: 23 substeps over free sites + 1 over the ROI (diffusion.cu:135-191).
 //     Each field is held in registers, two columns per lane: in the narrow
 //     kernel by a pair of warps whose half-warps hold four bands of rows
-//     (diffuse_half), in the wide kernel by four warps of one band each
+//     (diffuse_half), or, for regions up to 24 columns, whose eight-lane
+//     groups hold eight bands of two or three columns per lane
+//     (diffuse_band), in the wide kernel by four warps of one band each
 //     (diffuse_part).  Horizontal neighbours come from warp shuffles,
 //     vertical ones from the same thread's registers; bands swap one
 //     boundary row per substep (a shuffle across half-warps, shared memory
@@ -554,6 +556,120 @@ __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t 
   }
 }
 
+// Eight-lane bands for regions up to 8*C columns (no row or column offset):
+// lane = 8*bw + bl holds columns C*bl .. C*bl + C - 1, a warp holds four bands
+// of R rows (bw = 0..3), a field eight (band = 4*part + bw).  Horizontal
+// neighbours cost two shuffles per lane and row (one per lane edge); band
+// boundaries cross by shuffles up and down by 8 lanes inside a warp and
+// through shared memory between the two warps, with the producer/consumer
+// barriers of diffuse_half.  Same sites and expressions as diffuse_half, so
+// bit-identical results, with 4*R*C >= rows*cols/2 lane slots instead of
+// 2*ceil(rows/4)*32 for a region narrower than 17 (C = 2) or 25 (C = 3).
+template <int C, int R>
+__device__ __noinline__ void diffuse_band(float *__restrict__ f, const uint64_t *__restrict__ colmask,
+                                          float4 *__restrict__ xch, int part, int r0, int c0,
+                                          int h, int w, int nrow, int ncol, int W, float ext,
+                                          float ca, float cb, float cd, int nfree, int bar_id) {
+  constexpr int L = 8, K = 4;
+  const int lane = threadIdx.x & 31, bw = lane >> 3, bl = lane & 7;
+  const int band = part * K + bw;
+  const int base = band * R;  // region row of register row 0
+  const int left = (lane & ~7) | ((bl + 7) & 7), right = (lane & ~7) | ((bl + 1) & 7);
+  const uint32_t rowsel = (1u << R) - 1u;
+  const uint32_t roirows = (uint32_t)(((((1ull << h) - 1ull) << 1)) >> base) & rowsel;
+  const int lat0 = (r0 - 1) * W + (c0 - 1);
+  uint32_t fm[C], rm[C];
+  float X[C][R];
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const int j = C * bl + c;
+    fm[c] = (j < ncol) ? (uint32_t)(colmask[j] >> base) & rowsel : 0u;
+    rm[c] = (j >= 1 && j <= w) ? roirows : 0u;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int gi = base + i;
+      X[c][i] = (gi < nrow && j < ncol) ? (((fm[c] >> i) & 1u) ? f[lat0 + gi * W + j] : ext) : 0.f;
+    }
+  }
+  // boundary G between the two warps, C per lane: slot (parity, part) holds
+  // part 0's last row (its band 3) or part 1's first row (its band 0)
+  float *xs = reinterpret_cast<float *>(xch);
+  const bool writes = (part == 0) ? bw == K - 1 : bw == 0;
+  for (int s = 0; s <= nfree; ++s) {
+    const bool fin = (s == nfree);
+    const int par = s & 1;
+    float hs[C][R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const float lv = __shfl_sync(kFull, X[C - 1][i], left);
+      const float rv = __shfl_sync(kFull, X[0][i], right);
+#pragma unroll
+      for (int c = 0; c < C; ++c)
+        hs[c][i] = (c == 0 ? lv : X[c > 0 ? c - 1 : 0][i]) + (c == C - 1 ? rv : X[c < C - 1 ? c + 1 : 0][i]);
+    }
+    float gf[C], gl[C], up[C], dn[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      gf[c] = fmaf(cd, hs[c][0], cb * X[c][0]);
+      gl[c] = fmaf(cd, hs[c][R - 1], cb * X[c][R - 1]);
+      up[c] = __shfl_up_sync(kFull, gl[c], L);    // the band above: its last row
+      dn[c] = __shfl_down_sync(kFull, gf[c], L);  // the band below: its first row
+    }
+    const int own = bar_id + par * 2 + part, other = bar_id + par * 2 + (1 - part);
+    if (writes) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) xs[((par * 2 + part) * L + bl) * C + c] = part == 0 ? gl[c] : gf[c];
+    }
+    named_arrive(own, 64);
+    float g_second[C], g_penult[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const uint32_t u = fin ? rm[c] : fm[c];
+      // rows 1 .. R-2 need only this band's G
+      float gm = gf[c];
+      float gc = R > 1 ? fmaf(cd, hs[c][R > 1 ? 1 : 0], cb * X[c][R > 1 ? 1 : 0]) : 0.f;
+      g_second[c] = gc;
+#pragma unroll
+      for (int i = 1; i < R - 1; ++i) {
+        const float gn = (i + 1 == R - 1) ? gl[c] : fmaf(cd, hs[c][i + 1], cb * X[c][i + 1]);
+        const float nv = fmaf(ca, X[c][i], fmaf(cb, hs[c][i], gm + gn));
+        if ((u >> i) & 1u) X[c][i] = nv;
+        gm = gc;
+        gc = gn;
+      }
+      g_penult[c] = R > 2 ? gm : gf[c];
+    }
+    named_barrier(other, 64);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const uint32_t u = fin ? rm[c] : fm[c];
+      const float pw = writes ? xs[((par * 2 + (1 - part)) * L + bl) * C + c] : 0.f;
+      // above the first row, below the last row
+      const float ab = band == 0 ? 0.f : (bw == 0 ? pw : up[c]);
+      const float be = band == 2 * K - 1 ? 0.f : (bw == K - 1 ? pw : dn[c]);
+      if (R == 1) {
+        const float nv = fmaf(ca, X[c][0], fmaf(cb, hs[c][0], ab + be));
+        if (u & 1u) X[c][0] = nv;
+      } else {
+        const float f0 = fmaf(ca, X[c][0], fmaf(cb, hs[c][0], ab + g_second[c]));
+        const float l0 = fmaf(ca, X[c][R - 1], fmaf(cb, hs[c][R - 1], g_penult[c] + be));
+        if (u & 1u) X[c][0] = f0;
+        if ((u >> (R - 1)) & 1u) X[c][R - 1] = l0;
+      }
+    }
+  }
+  // write back the ROI interior
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const int j = C * bl + c;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int gi = base + i;
+      if (gi >= 1 && gi <= h && j >= 1 && j <= w) f[lat0 + gi * W + j] = X[c][i];
+    }
+  }
+}
+
 // NP warps per field; warp w diffuses field w / NP, part w % NP.
 // The caller guarantees 2*NP*RH_max >= nrow and (WIDE_OK or ncol <= 31).
 template <int NP, bool WIDE_OK>
@@ -587,8 +703,30 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
     default: break;                    \
   }
   if constexpr (NP == 2) {
-    // narrow kernel: two columns per lane, four bands of R rows per field
+    // narrow kernel: two columns per lane, four bands of R rows per field,
+    // or eight-lane bands when that takes fewer lane slots
     const int R = (nrow - roff + 3) / 4;
+    if (roff == 0 && coff == 0 && ncol <= 24) {
+      const int R8 = (nrow + 7) / 8;  // nrow <= 32 without a row offset
+      const bool two = ncol <= 16;
+      if ((two ? 2 : 3) * R8 < 2 * R) {
+#define EMT6_BAND(CC, RR) \
+  diffuse_band<CC, RR>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf, bar)
+        switch (R8 * 2 + (two ? 0 : 1)) {
+          case 2: EMT6_BAND(2, 1); break;
+          case 3: EMT6_BAND(3, 1); break;
+          case 4: EMT6_BAND(2, 2); break;
+          case 5: EMT6_BAND(3, 2); break;
+          case 6: EMT6_BAND(2, 3); break;
+          case 7: EMT6_BAND(3, 3); break;
+          case 8: EMT6_BAND(2, 4); break;
+          case 9: EMT6_BAND(3, 4); break;
+          default: break;
+        }
+#undef EMT6_BAND
+        return;
+      }
+    }
 #define EMT6_HALF(RR) \
   diffuse_half<RR>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf, bar, roff, coff)
     switch (R) {
