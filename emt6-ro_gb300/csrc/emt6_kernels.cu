@@ -670,6 +670,123 @@ __device__ __noinline__ void diffuse_band(float *__restrict__ f, const uint64_t 
   }
 }
 
+// Half-warp bands of three columns per lane for the wide kernel's regions of
+// 32-48 columns and 41-48 rows: lane 16*half + hl holds columns 3*hl ..
+// 3*hl + 2, each of the four warps of a field two bands of R rows
+// (band = 2*part + half).  The two halves of a warp swap boundary G by a
+// shuffle, neighbouring warps through shared-memory slots (double-buffered by
+// substep parity) under one named barrier of the field's 128 threads per
+// substep, as in diffuse_part.  Same sites and expressions as diffuse_part,
+// so bit-identical results, with 18 lane slots per lane (R = 6) instead of 24
+// (RH = 12).
+template <int R>
+__device__ __noinline__ void diffuse_wband(float *__restrict__ f, const uint64_t *__restrict__ colmask,
+                                           float4 *__restrict__ xch, int part, int r0, int c0,
+                                           int h, int w, int nrow, int ncol, int W, float ext,
+                                           float ca, float cb, float cd, int nfree, int bar_id) {
+  constexpr int C = 3, NPW = 4;
+  const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+  const int band = part * 2 + half;
+  const int base = band * R;  // region row of register row 0
+  const int left = (lane & 16) | ((hl + 15) & 15), right = (lane & 16) | ((hl + 1) & 15);
+  const uint32_t rowsel = (1u << R) - 1u;
+  const uint32_t roirows = (uint32_t)(((((1ull << h) - 1ull) << 1)) >> base) & rowsel;
+  const int lat0 = (r0 - 1) * W + (c0 - 1);
+  uint32_t fm[C], rm[C];
+  float X[C][R];
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const int j = C * hl + c;
+    fm[c] = (j < ncol) ? (uint32_t)(colmask[j] >> base) & rowsel : 0u;
+    rm[c] = (j >= 1 && j <= w) ? roirows : 0u;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int gi = base + i;
+      X[c][i] = (gi < nrow && j < ncol) ? (((fm[c] >> i) & 1u) ? f[lat0 + gi * W + j] : ext) : 0.f;
+    }
+  }
+  // exchange slot of (parity, warp, side): side 0 = the warp's first row (its
+  // first half-warp's row 0, read by the warp above), side 1 = its last row
+  // (read by the warp below); C floats per lane of a half-warp
+  auto slot = [&](int par, int pt, int side) -> float * {
+    return reinterpret_cast<float *>(xch) + (((par * NPW + pt) * 2 + side) * 16 + hl) * C;
+  };
+  for (int s = 0; s <= nfree; ++s) {
+    const bool fin = (s == nfree);
+    const int par = s & 1;
+    float hs[C][R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const float lv = __shfl_sync(kFull, X[C - 1][i], left);
+      const float rv = __shfl_sync(kFull, X[0][i], right);
+#pragma unroll
+      for (int c = 0; c < C; ++c)
+        hs[c][i] = (c == 0 ? lv : X[c > 0 ? c - 1 : 0][i]) + (c == C - 1 ? rv : X[c < C - 1 ? c + 1 : 0][i]);
+    }
+    float gf[C], gl[C], rc[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      gf[c] = fmaf(cd, hs[c][0], cb * X[c][0]);
+      gl[c] = fmaf(cd, hs[c][R - 1], cb * X[c][R - 1]);
+      // the first half-warp sends its last row's G, the second its first row's
+      rc[c] = __shfl_xor_sync(kFull, half ? gf[c] : gl[c], 16);
+    }
+    if (half == 0 && part > 0) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) slot(par, part, 0)[c] = gf[c];
+    }
+    if (half == 1 && part < NPW - 1) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) slot(par, part, 1)[c] = gl[c];
+    }
+    named_barrier(bar_id, NPW * 32);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const uint32_t u = fin ? rm[c] : fm[c];
+      // the warp above's last row (first half-warp) or the warp below's first
+      // row (second half-warp); zero beyond the field's first and last band
+      float pw = 0.f;
+      if (half == 0 && part > 0) pw = slot(par, part - 1, 1)[c];
+      if (half == 1 && part < NPW - 1) pw = slot(par, part + 1, 0)[c];
+      const float ab = half ? rc[c] : pw;  // above the first row
+      const float be = half ? pw : rc[c];  // below the last row
+      if (R == 1) {
+        const float nv = fmaf(ca, X[c][0], fmaf(cb, hs[c][0], ab + be));
+        if (u & 1u) X[c][0] = nv;
+      } else {
+        // rows 1 .. R-2, then the first and last rows (their G taken before
+        // any row of the band changes)
+        float gm = gf[c];
+        float gc = fmaf(cd, hs[c][R > 1 ? 1 : 0], cb * X[c][R > 1 ? 1 : 0]);
+        const float g_second = gc;
+#pragma unroll
+        for (int i = 1; i < R - 1; ++i) {
+          const float gn = (i + 1 == R - 1) ? gl[c] : fmaf(cd, hs[c][i + 1], cb * X[c][i + 1]);
+          const float nv = fmaf(ca, X[c][i], fmaf(cb, hs[c][i], gm + gn));
+          if ((u >> i) & 1u) X[c][i] = nv;
+          gm = gc;
+          gc = gn;
+        }
+        const float g_penult = R > 2 ? gm : gf[c];
+        const float f0 = fmaf(ca, X[c][0], fmaf(cb, hs[c][0], ab + g_second));
+        const float l0 = fmaf(ca, X[c][R - 1], fmaf(cb, hs[c][R - 1], g_penult + be));
+        if (u & 1u) X[c][0] = f0;
+        if ((u >> (R - 1)) & 1u) X[c][R - 1] = l0;
+      }
+    }
+  }
+  // write back the ROI interior
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const int j = C * hl + c;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int gi = base + i;
+      if (gi >= 1 && gi <= h && j >= 1 && j <= w) f[lat0 + gi * W + j] = X[c][i];
+    }
+  }
+}
+
 // NP warps per field; warp w diffuses field w / NP, part w % NP.
 // The caller guarantees 2*NP*RH_max >= nrow and (WIDE_OK or ncol <= 31).
 template <int NP, bool WIDE_OK>
@@ -743,6 +860,12 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
 #undef EMT6_HALF
   } else if (!WIDE_OK || ncol <= 31) {
     EMT6_CASES(false)
+  } else if (ncol <= 48 && nrow > 40 && nrow <= 48) {
+    // 32-48 columns and 41-48 rows: half-warp bands of three columns per lane
+    // (6 rows each) instead of 12-row tiles of two columns per lane.  Shorter
+    // bands do not pay for their per-substep exchange: measured slower than
+    // the 10-row tiles at 33-40 rows.
+    diffuse_wband<6>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf, bar);
   } else {
     EMT6_CASES(WIDE_OK)
   }
