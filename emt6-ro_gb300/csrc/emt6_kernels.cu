@@ -16,7 +16,8 @@
 //     (diffuse_half), or, for regions up to 24 columns, whose eight-lane
 //     groups hold eight bands of two or three columns per lane
 //     (diffuse_band), in the wide kernel by four warps of one band each
-//     (diffuse_part).  Horizontal neighbours come from warp shuffles,
+//     (diffuse_part) or, for 41-48 rows, half-warp bands of three columns
+//     per lane (diffuse_wband).  Horizontal neighbours come from warp shuffles,
 //     vertical ones from the same thread's registers; bands swap one
 //     boundary row per substep (a shuffle across half-warps, shared memory
 //     between warps under 64- or 128-thread named barriers).
