@@ -252,6 +252,12 @@ __device__ void restore_colmask(uint64_t *colmask, const Misc *m) {
 // rotating shuffle hands lane 0 the value of column 32, which equals that of
 // column 0 (both fixed at the external level).  Likewise a 33-high region with
 // an entirely fixed first row holds rows 1..32; row 0 becomes a constant.
+// The rotating shuffle also hands column 0 its left neighbour and the last
+// column its right one: a column beyond the region (zero, like the ring
+// outside the tile) while the region has fewer columns than the lanes hold,
+// but the opposite ring column in a 32-wide region.  That is only right when
+// both ring columns are fixed; a clipped ROI (against the lattice edge) can
+// leave ring sites free, and such a 32-wide region goes to the wide kernel.
 // Called by one thread.
 __device__ void narrow_mapping(const uint64_t *colmask, Misc *m) {
   const int nrow = m->roi[2] + 2, ncol = m->roi[3] + 2;
@@ -265,6 +271,7 @@ __device__ void narrow_mapping(const uint64_t *colmask, Misc *m) {
       if (colmask[0] != 0 || colmask[32] != 0) ok = 0;
       coff = 1;
     }
+    if (ncol == 32 && (colmask[0] != 0 || colmask[31] != 0)) ok = 0;
     if (nrow == 33) {
       uint64_t first = 0;
       for (int j = 0; j < ncol; ++j) first |= colmask[j] & 1ull;
@@ -557,15 +564,17 @@ __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t 
   }
 }
 
-// Eight-lane bands for regions up to 8*C columns (no row or column offset):
+// Eight-lane bands for regions up to 8*C - 1 columns (no row or column
+// offset; the spare lane column is the zero left neighbour of column 0):
 // lane = 8*bw + bl holds columns C*bl .. C*bl + C - 1, a warp holds four bands
 // of R rows (bw = 0..3), a field eight (band = 4*part + bw).  Horizontal
 // neighbours cost two shuffles per lane and row (one per lane edge); band
 // boundaries cross by shuffles up and down by 8 lanes inside a warp and
 // through shared memory between the two warps, with the producer/consumer
 // barriers of diffuse_half.  Same sites and expressions as diffuse_half, so
-// bit-identical results, with 4*R*C >= rows*cols/2 lane slots instead of
-// 2*ceil(rows/4)*32 for a region narrower than 17 (C = 2) or 25 (C = 3).
+// bit-identical results, with C*R lane slots per lane (R = ceil(rows/8))
+// instead of 2*ceil(rows/4), for regions up to 15 (C = 2) or 23 (C = 3)
+// columns.
 template <int C, int R>
 __device__ __noinline__ void diffuse_band(float *__restrict__ f, const uint64_t *__restrict__ colmask,
                                           float4 *__restrict__ xch, int part, int r0, int c0,
@@ -672,7 +681,7 @@ __device__ __noinline__ void diffuse_band(float *__restrict__ f, const uint64_t 
 }
 
 // Half-warp bands of three columns per lane for the wide kernel's regions of
-// 32-48 columns and 41-48 rows: lane 16*half + hl holds columns 3*hl ..
+// 32-47 columns and 41-48 rows: lane 16*half + hl holds columns 3*hl ..
 // 3*hl + 2, each of the four warps of a field two bands of R rows
 // (band = 2*part + half).  The two halves of a warp swap boundary G by a
 // shuffle, neighbouring warps through shared-memory slots (double-buffered by
@@ -824,9 +833,11 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
     // narrow kernel: two columns per lane, four bands of R rows per field,
     // or eight-lane bands when that takes fewer lane slots
     const int R = (nrow - roff + 3) / 4;
-    if (roff == 0 && coff == 0 && ncol <= 24) {
+    // (a band layout needs a spare lane column: the shuffle that fetches
+    // column 0's left neighbour then wraps to a zero column)
+    if (roff == 0 && coff == 0 && ncol <= 23) {
       const int R8 = (nrow + 7) / 8;  // nrow <= 32 without a row offset
-      const bool two = ncol <= 16;
+      const bool two = ncol <= 15;
       if ((two ? 2 : 3) * R8 < 2 * R) {
 #define EMT6_BAND(CC, RR) \
   diffuse_band<CC, RR>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf, bar)
@@ -861,8 +872,9 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
 #undef EMT6_HALF
   } else if (!WIDE_OK || ncol <= 31) {
     EMT6_CASES(false)
-  } else if (ncol <= 48 && nrow > 40 && nrow <= 48) {
-    // 32-48 columns and 41-48 rows: half-warp bands of three columns per lane
+  } else if (ncol <= 47 && nrow > 40 && nrow <= 48) {
+    // 32-47 columns (a spare lane column for the wrap of column 0's left
+    // neighbour) and 41-48 rows: half-warp bands of three columns per lane
     // (6 rows each) instead of 12-row tiles of two columns per lane.  Shorter
     // bands do not pay for their per-substep exchange: measured slower than
     // the 10-row tiles at 33-40 rows.

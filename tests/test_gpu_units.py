@@ -179,17 +179,12 @@ def test_list_and_roi_match_oracle(case, oracle):
     assert (mask[:m] == mo[:m]).all()
 
 
-@pytest.mark.parametrize("case", range(10))
-def test_diffusion_step_parity(case, params, oracle):
-    """One diffusion step (23 free substeps + final ROI pass): bit-exact against
-    the oracle's FP32 formula on both kernel paths, and within 1e-5 relative of
-    the reference formula evaluated in FP64."""
+def _diffusion_parity(st, rng, params, oracle):
+    """One diffusion step of lattice st's ROI on both kernel paths: bit-exact
+    against the oracle's FP32 formula and within 1e-5 relative of the FP64
+    evaluation of the reference formula.  Returns (rows, columns, paths run)."""
     N = _N()
-    rng = np.random.default_rng(200 + case)
-    H = W = 53
-    radius = [3, 6, 9, 11, 13, 14, 16, 19, 22, 26][case]
-    center = (26 + int(rng.integers(-4, 5)), 26 + int(rng.integers(-4, 5)))
-    st = _random_lattice(rng, H, W, radius, center, density=0.95)
+    H, W = st.shape
     L = oracle.oracle().L
     roi = np.zeros(5, np.int32)
     mask = np.zeros(H * W + 512, np.uint8)
@@ -227,5 +222,55 @@ def test_diffusion_step_parity(case, params, oracle):
             assert rel.max() <= 1e-5, (v, f, rel.max())
     if nrow <= 32 and ncol <= 31:
         assert ran == [0, 1]
+    return nrow, ncol, ran
+
+
+@pytest.mark.parametrize("case", range(10))
+def test_diffusion_step_parity(case, params, oracle):
+    """One diffusion step (23 free substeps + final ROI pass) of near-centred
+    discs from 9 x 9 to 55 x 55 regions."""
+    rng = np.random.default_rng(200 + case)
+    H = W = 53
+    radius = [3, 6, 9, 11, 13, 14, 16, 19, 22, 26][case]
+    center = (26 + int(rng.integers(-4, 5)), 26 + int(rng.integers(-4, 5)))
+    st = _random_lattice(rng, H, W, radius, center, density=0.95)
+    nrow, ncol, ran = _diffusion_parity(st, rng, params, oracle)
     if radius in (13, 14):
         assert 0 in ran  # 31-wide unclipped ROI: the shifted narrow mapping
+
+
+# Tumours against the lattice edge: ROIs clipped to fewer columns than rows,
+# which reach the register layouts a centred disc does not (eight-lane bands
+# of 2 columns with 3-4 rows and of 3 columns with 4 rows, the wide kernel's
+# three-column bands on a 41 x 32 region, two-column wide tiles of 14 rows),
+# and clipped regions exactly as wide as a layout's lanes hold columns
+# (16, 24, 32, 48) with free sites in a ring column: the shuffle that fetches
+# column 0's left neighbour must not wrap to the opposite ring column there.
+# (radius, centre, seed, expected rows x columns)
+_CLIPPED = [(4, (26, 2), 1402, (13, 11)), (6, (26, 2), 1602, (17, 14)),
+            (6, (26, 20), 1620, (17, 17)), (9, (26, 5), 1905, (25, 21)),
+            (11, (26, 7), 2107, (29, 25)), (13, (26, 2), 2302, (33, 25)),
+            (16, (26, 4), 2604, (41, 32)), (17, (26, 2), 2702, (41, 31)),
+            (19, (26, 9), 2909, (49, 40)), (6, (26, 4), 1604, (19, 16)),
+            (10, (26, 8), 2008, (27, 24)), (13, (3, 13), 135313, (27, 32)),
+            (20, (8, 22), 205822, (41, 48))]
+# strips of occupied sites along the left edge: (columns, expected shape)
+_STRIPS = [(1, (25, 14)), (2, (27, 16))]
+
+
+@pytest.mark.parametrize("case", range(len(_CLIPPED) + len(_STRIPS)))
+def test_diffusion_clipped_regions(case, params, oracle):
+    H = W = 53
+    if case < len(_CLIPPED):
+        radius, center, seed, shape = _CLIPPED[case]
+        rng = np.random.default_rng(seed)
+        st = _random_lattice(rng, H, W, radius, center, density=0.95)
+    else:
+        # 23 rows of one or two columns: a 25 x 14 or 27 x 16 region
+        cols, shape = _STRIPS[case - len(_CLIPPED)]
+        rng = np.random.default_rng(77 + cols)
+        st = np.zeros((H, W), np.uint8)
+        st[0, :] = st[-1, :] = st[:, 0] = st[:, -1] = 2
+        st[14:37, 1:1 + cols] = 1
+    nrow, ncol, _ = _diffusion_parity(st, rng, params, oracle)
+    assert (nrow, ncol) == shape
