@@ -49,6 +49,23 @@ def test_small_batch_bit_exact(params, oracle):
     _assert_same(b, ob, len(st))
 
 
+def test_tumours_against_the_lattice_edge_bit_exact(params, oracle):
+    """Tumours in a corner and against the edges: clipped ROIs (even-sized
+    regions, ring sites left free by the mask), divisions next to the mocked
+    border, and regions that leave the narrow kernel for the wide one."""
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, 7, seed=11, center=(6, 6)),
+              wl.disc_tumor(params, 10, seed=12, center=(26, 3)),
+              wl.disc_tumor(params, 14, seed=13, center=(45, 30)),
+              wl.disc_tumor(params, 18, seed=14, center=(26, 8))]
+    protocols = [[], [(300, 2.0), (900, 1.5)]]
+    st = np.array([0, 1, 2, 3, 0, 1, 2, 3], np.int32)
+    sp = np.array([0, 0, 0, 0, 1, 1, 1, 1], np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 1500, seed=91)
+    assert (c == co).all(), (c, co)
+    _assert_same(b, ob, len(st))
+
+
 def test_chunked_runs_equal_one_run(params, oracle):
     from emt6ro import workloads as wl
     tumors = [wl.disc_tumor(params, 10, seed=9)]
