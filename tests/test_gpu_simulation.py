@@ -66,6 +66,26 @@ def test_tumours_against_the_lattice_edge_bit_exact(params, oracle):
     _assert_same(b, ob, len(st))
 
 
+@pytest.mark.parametrize("dims", [(40, 47), (54, 60)])
+def test_other_lattice_sizes_bit_exact(oracle, dims):
+    """Interiors other than 51 x 51, up to the largest the kernels hold
+    (54 x 60): a non-square lattice, a tumour against its edge and one whose
+    region needs the wide kernel."""
+    from emt6ro import workloads as wl
+    p = wl.default_parameters()
+    p.native.lattice_height, p.native.lattice_width = dims
+    H, W = dims[0] + 2, dims[1] + 2
+    tumors = [wl.disc_tumor(p, 9, seed=21, center=(H // 2, W // 2)),
+              wl.disc_tumor(p, 8, seed=22, center=(H // 2, 3)),
+              wl.disc_tumor(p, 19, seed=23, center=(H // 2, W // 2))]
+    protocols = [[], [(120, 2.5)]]
+    st = np.array([0, 1, 2, 0, 1, 2], np.int32)
+    sp = np.array([0, 0, 0, 1, 1, 1], np.int32)
+    b, ob, c, co = _run_pair(p, oracle, tumors, protocols, st, sp, 600, seed=57)
+    assert (c == co).all(), (c, co)
+    _assert_same(b, ob, len(st))
+
+
 def test_chunked_runs_equal_one_run(params, oracle):
     from emt6ro import workloads as wl
     tumors = [wl.disc_tumor(params, 10, seed=9)]
