@@ -86,6 +86,25 @@ def test_other_lattice_sizes_bit_exact(oracle, dims):
     _assert_same(b, ob, len(st))
 
 
+def test_empty_and_single_cell_lattices_bit_exact(params, oracle):
+    """No cell at all (empty list, 0 x 0 ROI from the first step) and a single
+    cell in a corner and in the middle (3 x 3 regions), irradiated or not."""
+    from emt6ro import workloads as wl
+    import emt6ro.simulation as sim
+    empty = wl.disc_tumor(params, 0, seed=41).sites.copy()
+    empty["state"][1:-1, 1:-1] = 0
+    corner = wl.disc_tumor(params, 0, seed=42, center=(1, 1))
+    middle = wl.disc_tumor(params, 0, seed=43)
+    tumors = [sim.TumorState(empty), corner, middle]
+    protocols = [[], [(0, 3.0)]]
+    st = np.array([0, 1, 2, 0, 1, 2], np.int32)
+    sp = np.array([0, 0, 0, 1, 1, 1], np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 3000, seed=23)
+    assert (c == co).all(), (c, co)
+    assert c[0] == 0 and c[3] == 0
+    _assert_same(b, ob, len(st))
+
+
 def test_chunked_runs_equal_one_run(params, oracle):
     from emt6ro import workloads as wl
     tumors = [wl.disc_tumor(params, 10, seed=9)]
