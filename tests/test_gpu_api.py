@@ -64,6 +64,34 @@ def test_experiment_matches_batch_and_oracle(setup, oracle):
     assert (r.reshape(-1) == ob.counts()).all()
 
 
+def test_experiment_other_resolution_and_length(setup, oracle):
+    """simulation_steps = 6,000 and protocol_resolution = 60: doses accumulate
+    in bin step // 60 and fire at its first step; a run past the protocol
+    length gives no further doses (protocol.h:9-18)."""
+    import emt6ro.simulation as sim
+    from emt6ro import workloads as wl
+    params, tumors = setup
+    prots = [[(0, 1.0), (90, 1.0), (130, 0.5), (5999, 2.0)], [(59, 3.0), (4200, 1.0)]]
+    e = sim.Experiment(params, tumors, 2, 2, 0, 6000, 60, seed=29)
+    e.add_irradiations(prots)
+    with pytest.raises(RuntimeError, match="beyond the protocol length"):
+        e.add_irradiations([[(6000, 1.0)], []])
+    e.run(6600)
+    r = e.get_results()
+    dose = wl.protocol_doses(prots, 100, 60)
+    assert dose[0][1] == 1.0 and dose[0][2] == 0.5 and dose[0][99] == 2.0
+    assert dose[1][0] == 3.0 and dose[1][70] == 1.0
+    ob = oracle.Batch(oracle.params_copy(params), 8, 29)
+    i = 0
+    for p in range(2):
+        for t in range(2):
+            for _ in range(2):
+                ob.set(i, tumors[t].sites, dose[p], resolution=60, length=6000)
+                i += 1
+    ob.run(6600, nthreads=8)
+    assert (r.reshape(-1) == ob.counts()).all()
+
+
 def test_reset_restores_initial_states(setup):
     import emt6ro.simulation as sim
     params, tumors = setup
