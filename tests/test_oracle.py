@@ -239,11 +239,14 @@ def test_diffusion_f32_within_1e5_of_f64(params, oracle):
     L = oracle.oracle().L
     rng = np.random.default_rng(5)
     H = W = 53
-    for rad in (4, 10, 14, 20):
+    # centred discs, and discs against the lattice edge (clipped ROIs whose
+    # ring sites the mask can leave free, next to the zero ring of the tile)
+    for rad, (cr, ccol) in ((4, (26, 26)), (10, (26, 26)), (14, (26, 26)), (20, (26, 26)),
+                            (10, (26, 3)), (7, (3, 3)), (14, (45, 30)), (20, (8, 22))):
         st = np.zeros((H, W), np.uint8)
         st[0, :] = st[-1, :] = st[:, 0] = st[:, -1] = 2
         rr, cc = np.mgrid[0:H, 0:W]
-        st[((rr - 26) ** 2 + (cc - 26) ** 2 <= rad * rad) & (st != 2)] = 1
+        st[((rr - cr) ** 2 + (cc - ccol) ** 2 <= rad * rad) & (st != 2)] = 1
         roi = np.zeros(5, np.int32)
         mask = np.zeros(H * W + 512, np.uint8)
         L.orc_find_roi(np.ascontiguousarray(st.reshape(-1)), H, W, roi, mask)
