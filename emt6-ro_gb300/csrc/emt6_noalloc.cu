@@ -1,11 +1,11 @@
 // emt6_noalloc.cu -- a simulation entry point that allocates no device memory.
 //
-// emt6_simulate_noalloc serves callers that cannot call cudaMalloc: code that
-// runs while its stream is being captured into a CUDA graph (allocation is not
-// allowed there), or code embedded in a host framework whose allocator owns
-// all device memory (a caching pool such as PyTorch's, where stray cudaMalloc
-// calls fragment the pool or exceed its budget).  Such a caller hands over
-// device buffers it already owns -- the initial lattices, the dose table, the
+// emt6_simulate_noalloc serves callers that cannot call cudaMalloc: code
+// embedded in a host application or framework whose allocator owns all device
+// memory (a caching pool such as PyTorch's, where stray cudaMalloc calls
+// fragment the pool or push it past its budget), or a plug-in whose host
+// fixes every device allocation at start-up.  Such a caller hands over device
+// buffers it already owns -- the initial lattices, the dose table, the
 // simulation -> tumour/protocol maps and the output counts -- and the library
 // keeps each simulation's working state (fields, site states, cell records,
 // occupied list) in the file-scope array below, which every GPU that loads the
@@ -15,14 +15,19 @@
 //   * kNoAllocBytes (8 MiB) of working state per device: a default 53 x 53
 //     lattice takes about 177 KB per simulation, so one call runs at most 47
 //     of them; larger requests are rejected with EMT6_ERR_LIMIT.
-//   * The first call on a device looks the array's device address up (with
-//     that device current); make that first call before any stream capture.
+//   * The first call on a device (and the first one after the device's
+//     context was re-created, e.g. by cudaDeviceReset) looks the array's
+//     device address up with that device current; make that first call
+//     before any stream capture.
 //   * All calls share the one array and it keeps the last call's contents;
 //     every call re-initialises the state it uses.  Calls that overlap on the
 //     GPU (concurrent streams, or host threads racing on one device) race on
 //     it: serialise them.
-//   * The call enqueues its kernels on the given stream and waits for them, so
-//     it can report a device-side error flag.
+//   * The call enqueues its kernels on the given stream, then copies the
+//     device error flag to the host and synchronises that stream, so it
+//     returns only when the counts are written.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -40,7 +45,10 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 std::mutex g_mu;
+// per device: the scratch array's address and the id of the context it was
+// looked up in (0 = not looked up yet)
 void *g_scratch_addr[kMaxDevices] = {nullptr};
+unsigned long long g_scratch_ctx[kMaxDevices] = {0};
 
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
@@ -109,16 +117,48 @@ __global__ void noalloc_count_kernel(const uint8_t *st, uint32_t sstride, int HW
   }
 }
 
-// Device address of the scratch array for the current device (looked up once).
+// Id of the context current on this thread (0 when there is none or the
+// driver does not report ids).  Context ids are unique for the life of the
+// process, so a re-created context never matches an old one.
+unsigned long long current_context_id() {
+  static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(f);
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of the scratch array on the current device.  The set-up
+// (cudaGetSymbolAddress with the device current) runs once per device and
+// again whenever the device's context has been re-created since, because the
+// module, and with it the array, may then sit at another address.
 int scratch_address(int device, unsigned char **out) {
   if (device < 0 || device >= kMaxDevices) return fail(EMT6_ERR_INVALID, "device id too large");
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[device]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_scratch_addr[device] || ctx == 0 || ctx != g_scratch_ctx[device]) {
     void *ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess)
       return fail(EMT6_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     g_scratch_addr[device] = ptr;
+    // the lookup made the device's context current on this thread
+    g_scratch_ctx[device] = current_context_id();
   }
   *out = static_cast<unsigned char *>(g_scratch_addr[device]);
   return EMT6_OK;

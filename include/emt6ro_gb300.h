@@ -195,21 +195,23 @@ int emt6_test_diffuse(const emt6_params *p, float *fields, int32_t height, int32
 
 /* ---- allocation-free entry point -------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:
- * code issuing work while its stream is captured into a CUDA graph, or code
- * inside a framework whose allocator owns all device memory.  Every pointer
- * argument except p is a DEVICE pointer the caller owns: d_tumors
- * (n_tumors x height x width emt6_site), d_sim_tumor / d_sim_protocol
- * (n_sims int32), d_doses (n_protocols x protocol_bins float) and the output
- * d_counts (n_sims uint32).  Runs nsteps steps of every simulation from its
- * initial lattice (random stream keyed by seed, simulation index and epoch 0,
- * so the counts equal those of emt6_batch_* on the same inputs) on the given
- * cudaStream_t on the current device, waits for it, and returns.
+ * code inside a host application or framework whose allocator owns all device
+ * memory (a caching pool, or a host that fixes every device allocation at
+ * start-up).  Every pointer argument except p is a DEVICE pointer the caller
+ * owns: d_tumors (n_tumors x height x width emt6_site), d_sim_tumor /
+ * d_sim_protocol (n_sims int32), d_doses (n_protocols x protocol_bins float)
+ * and the output d_counts (n_sims uint32).  Runs nsteps steps of every
+ * simulation from its initial lattice (random stream keyed by seed,
+ * simulation index and epoch 0, so the counts equal those of emt6_batch_* on
+ * the same inputs) on the given cudaStream_t on the current device, then
+ * synchronises that stream and returns.
  * The working state lives in a fixed 8 MiB device array inside the library
  * (held by every GPU that loads it until exit): at most 47 simulations of the
  * default 53 x 53 lattice per call; larger requests fail with EMT6_ERR_LIMIT.
- * The first call on a device looks the array's address up: make it before
- * any stream capture.  Calls share the array; calls that overlap on the GPU
- * race on it. */
+ * The first call on a device (and the first after its context is re-created)
+ * looks the array's address up: make it before any stream capture.  All calls
+ * share the array; calls that overlap on the GPU race on it, so serialise
+ * them across streams and threads. */
 int emt6_simulate_noalloc(const emt6_params *p, const emt6_site *d_tumors, int32_t height,
                           int32_t width, const int32_t *d_sim_tumor,
                           const int32_t *d_sim_protocol, int64_t n_sims, const float *d_doses,

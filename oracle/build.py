@@ -29,7 +29,9 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE_ROOT = Path(os.environ.get("EMT6_REFERENCE_ROOT", "/root/reference"))
+# the reference checkout: $EMT6_REFERENCE_ROOT, else a sibling directory of
+# this repository named "reference"
+REFERENCE_ROOT = Path(os.environ.get("EMT6_REFERENCE_ROOT") or HERE.parent.parent / "reference")
 CUDA_INC = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
 
 ORACLE_LIB = BUILD / "liborc.so"
@@ -62,7 +64,7 @@ def build_oracle(force: bool = False) -> Path:
     srcs = [HERE / "emt6_oracle.c", HERE / "emt6_oracle.h"]
     if force or _stale(ORACLE_LIB, srcs):
         tmp = ORACLE_LIB.with_suffix(".so.tmp")
-        _run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", *_arch_flags(), "-fPIC",
+        _run(["gcc", "-O3", "-std=gnu11", "-ffp-contract=off", *_arch_flags(), "-fPIC",
               "-shared", "-o", str(tmp), str(HERE / "emt6_oracle.c"), "-lm", "-lpthread"])
         os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
@@ -85,7 +87,7 @@ def build_ref(force: bool = False) -> Path | None:
         return REF_LIB
     inc = ["-I", str(src), "-I", str(REFERENCE_ROOT / "third-party" / "json"),
            "-I", str(CUDA_INC), "-I", str(HERE)]
-    common = ["-O2", "-DNDEBUG", "-ffp-contract=off", "-fPIC"]
+    common = ["-O3", "-DNDEBUG", "-ffp-contract=off", "-fPIC", *_arch_flags()]
     objs = []
     for s in ref_srcs:
         o = REF_OUT / (s.stem + ".o")

@@ -449,6 +449,34 @@ void orc_diffusion_coeffs(const orc_params *p, float k[3], float a[3], float b[3
  * (r0-1+i, c0-1+j); padded by one zero ring (the reference's outer ring). */
 #define ORC_TILE(T, i, j) T[((i) + 1) * tw + ((j) + 1)]
 
+/* a where m is all ones, b where m is zero (a bitwise blend, so the loops
+ * using it have no branches and vectorise) */
+static inline float orc_sel(int32_t m, float a, float b) {
+  uint32_t ua, ub;
+  memcpy(&ua, &a, 4);
+  memcpy(&ub, &b, 4);
+  const uint32_t r = (ua & (uint32_t)m) | (ub & ~(uint32_t)m);
+  float f;
+  memcpy(&f, &r, 4);
+  return f;
+}
+
+/* Which tile sites a substep updates, as all-ones / zero words so the update
+ * loops below are branch-free (and vectorise): free substeps update the
+ * sites the mask leaves free, the final substep every ROI site (the interior
+ * of the ring).  Positions outside the region stay zero. */
+static void orc_update_masks(const uint8_t *mask, int h, int w, int tw, int tn, int32_t *ufree,
+                             int32_t *ufin) {
+  int nrow = h + 2, ncol = w + 2;
+  memset(ufree, 0, sizeof(int32_t) * tn);
+  memset(ufin, 0, sizeof(int32_t) * tn);
+  for (int i = 0; i < nrow; ++i)
+    for (int j = 0; j < ncol; ++j) {
+      ORC_TILE(ufree, i, j) = mask[i * ncol + j] ? 0 : -1;
+      ORC_TILE(ufin, i, j) = (i >= 1 && i <= h && j >= 1 && j <= w) ? -1 : 0;
+    }
+}
+
 void orc_diffuse_f32(float *fld, int H, int W, const int32_t roi[5], const uint8_t *mask,
                      const orc_params *p) {
   int r0 = roi[0], c0 = roi[1], h = roi[2], w = roi[3];
@@ -456,49 +484,63 @@ void orc_diffuse_f32(float *fld, int H, int W, const int32_t roi[5], const uint8
   float kk[3], a[3], b[3], d[3];
   int nsub;
   orc_diffusion_coeffs(p, kk, a, b, d, &nsub);
-  int nrow = h + 2, ncol = w + 2, tw = ncol + 2, tn = (nrow + 2) * tw;
+  /* rows of the tile are padded to a multiple of 8 columns (zero, never
+   * updated) so the substep loops have no remainder iterations */
+  int nrow = h + 2, ncol = w + 2, ncp = (ncol + 7) & ~7, tw = ncp + 2, tn = (nrow + 2) * tw;
+  /* X, Y: the field tile with the zero outer ring; Hs, G per site; the rows
+   * of G above and below the region stay zero (the ring's G) */
   float *X = (float *)calloc((size_t)tn, sizeof(float));
   float *Y = (float *)calloc((size_t)tn, sizeof(float));
   float *Hs = (float *)calloc((size_t)tn, sizeof(float));
   float *G = (float *)calloc((size_t)tn, sizeof(float));
+  int32_t *ufree = (int32_t *)malloc(sizeof(int32_t) * (size_t)tn);
+  int32_t *ufin = (int32_t *)malloc(sizeof(int32_t) * (size_t)tn);
+  orc_update_masks(mask, h, w, tw, tn, ufree, ufin);
   int nfree = nsub - 1 > 0 ? nsub - 1 : 0;
   for (int f = 0; f < 3; ++f) {
     float *L = fld + (size_t)f * H * W;
-    const float ext = p->external_levels[f];
+    const float ext = p->external_levels[f], fa = a[f], fb = b[f], fd = d[f];
     memset(X, 0, sizeof(float) * tn);
+    memset(Y, 0, sizeof(float) * tn);
     for (int i = 0; i < nrow; ++i)
       for (int j = 0; j < ncol; ++j)
         ORC_TILE(X, i, j) = mask[i * ncol + j] ? ext : L[(r0 - 1 + i) * W + (c0 - 1 + j)];
     for (int s = 0; s <= nfree; ++s) {
-      int final = (s == nfree);
+      const int32_t *U = (s == nfree) ? ufin : ufree;
       /* H = left + right, G = b*x + d*H (rounded as fmaf(d, H, b*x));
        * x' = a*x + b*(H + up + down) + d*(H_up + H_down)
        *    = fmaf(a, x, fmaf(b, H, G_up + G_down)) */
-      for (int i = -1; i <= nrow; ++i)
-        for (int j = 0; j < ncol; ++j) {
-          const float hs = ORC_TILE(X, i, j - 1) + ORC_TILE(X, i, j + 1);
-          ORC_TILE(Hs, i, j) = hs;
-          ORC_TILE(G, i, j) = fmaf(d[f], hs, b[f] * ORC_TILE(X, i, j));
+      for (int i = 0; i < nrow; ++i) {
+        const float *restrict x = &ORC_TILE(X, i, 0);
+        float *restrict hs = &ORC_TILE(Hs, i, 0), *restrict g = &ORC_TILE(G, i, 0);
+        for (int j = 0; j < ncp; ++j) {
+          const float hv = x[j - 1] + x[j + 1];
+          hs[j] = hv;
+          g[j] = fmaf(fd, hv, fb * x[j]);
         }
-      memcpy(Y, X, sizeof(float) * tn);
-      for (int i = 0; i < nrow; ++i)
-        for (int j = 0; j < ncol; ++j) {
-          int upd = final ? (i >= 1 && i <= h && j >= 1 && j <= w) : !mask[i * ncol + j];
-          if (!upd) continue;
-          ORC_TILE(Y, i, j) = fmaf(a[f], ORC_TILE(X, i, j),
-                                   fmaf(b[f], ORC_TILE(Hs, i, j),
-                                        ORC_TILE(G, i - 1, j) + ORC_TILE(G, i + 1, j)));
+      }
+      for (int i = 0; i < nrow; ++i) {
+        const float *restrict x = &ORC_TILE(X, i, 0), *restrict hs = &ORC_TILE(Hs, i, 0);
+        const float *restrict gu = &ORC_TILE(G, i - 1, 0), *restrict gd = &ORC_TILE(G, i + 1, 0);
+        const int32_t *restrict u = &ORC_TILE(U, i, 0);
+        float *restrict y = &ORC_TILE(Y, i, 0);
+        for (int j = 0; j < ncp; ++j) {
+          const float nv = fmaf(fa, x[j], fmaf(fb, hs[j], gu[j] + gd[j]));
+          y[j] = orc_sel(u[j], nv, x[j]);
         }
+      }
       float *tmp = X; X = Y; Y = tmp;
     }
     for (int i = 1; i <= h; ++i)
       for (int j = 1; j <= w; ++j) L[(r0 - 1 + i) * W + (c0 - 1 + j)] = ORC_TILE(X, i, j);
   }
-  free(X); free(Y); free(Hs); free(G);
+  free(X); free(Y); free(Hs); free(G); free(ufree); free(ufin);
 }
 
 /* The reference's own expression (diffusion.cu:122-133) in FP32, used by the
- * ORC_REF_CELL build for the reference CPU path. */
+ * ORC_REF_CELL build for the reference CPU path.  The increment of every
+ * site is computed from the substep's old values, then added where the
+ * substep updates (diffusion.cu:172-188). */
 static void orc_diffuse_ref_f32(float *fld, int H, int W, const int32_t roi[5],
                                 const uint8_t *mask, const orc_params *p) {
   int r0 = roi[0], c0 = roi[1], h = roi[2], w = roi[3];
@@ -508,41 +550,48 @@ static void orc_diffuse_ref_f32(float *fld, int H, int W, const int32_t roi[5],
   orc_diffusion_coeffs(p, kk, a, b, d, &nsub);
   const float S2 = (float)0.70710678118654752440;
   const float F = (float)(4. + (double)(float)(2 * 1.41421356237309504880));
-  int nrow = h + 2, ncol = w + 2, tw = ncol + 2, tn = (nrow + 2) * tw;
+  /* rows of the tile are padded to a multiple of 8 columns (zero, never
+   * updated) so the substep loops have no remainder iterations */
+  int nrow = h + 2, ncol = w + 2, ncp = (ncol + 7) & ~7, tw = ncp + 2, tn = (nrow + 2) * tw;
   float *X = (float *)calloc((size_t)tn, sizeof(float));
   float *D = (float *)calloc((size_t)tn, sizeof(float));
+  int32_t *ufree = (int32_t *)malloc(sizeof(int32_t) * (size_t)tn);
+  int32_t *ufin = (int32_t *)malloc(sizeof(int32_t) * (size_t)tn);
+  orc_update_masks(mask, h, w, tw, tn, ufree, ufin);
   int nfree = nsub - 1 > 0 ? nsub - 1 : 0;
   for (int f = 0; f < 3; ++f) {
     float *L = fld + (size_t)f * H * W;
+    const float k = kk[f];
     memset(X, 0, sizeof(float) * tn);
     for (int i = 0; i < nrow; ++i)
       for (int j = 0; j < ncol; ++j)
         ORC_TILE(X, i, j) =
             mask[i * ncol + j] ? p->external_levels[f] : L[(r0 - 1 + i) * W + (c0 - 1 + j)];
     for (int s = 0; s <= nfree; ++s) {
-      int final = (s == nfree);
-      for (int i = 0; i < nrow; ++i)
-        for (int j = 0; j < ncol; ++j) {
-          int upd = final ? (i >= 1 && i <= h && j >= 1 && j <= w) : !mask[i * ncol + j];
-          if (!upd) continue;
-          float res = ORC_TILE(X, i - 1, j) + ORC_TILE(X, i, j - 1) + ORC_TILE(X, i + 1, j) +
-                      ORC_TILE(X, i, j + 1);
-          res += (ORC_TILE(X, i - 1, j - 1) + ORC_TILE(X, i - 1, j + 1) +
-                  ORC_TILE(X, i + 1, j - 1) + ORC_TILE(X, i + 1, j + 1)) * S2;
-          res -= ORC_TILE(X, i, j) * F;
-          res *= kk[f];
-          ORC_TILE(D, i, j) = res;
+      const int32_t *U = (s == nfree) ? ufin : ufree;
+      for (int i = 0; i < nrow; ++i) {
+        const float *restrict xu = &ORC_TILE(X, i - 1, 0), *restrict x = &ORC_TILE(X, i, 0);
+        const float *restrict xd = &ORC_TILE(X, i + 1, 0);
+        float *restrict dd = &ORC_TILE(D, i, 0);
+        for (int j = 0; j < ncp; ++j) {
+          float res = xu[j] + x[j - 1] + xd[j] + x[j + 1];
+          res += (xu[j - 1] + xu[j + 1] + xd[j - 1] + xd[j + 1]) * S2;
+          res -= x[j] * F;
+          res *= k;
+          dd[j] = res;
         }
-      for (int i = 0; i < nrow; ++i)
-        for (int j = 0; j < ncol; ++j) {
-          int upd = final ? (i >= 1 && i <= h && j >= 1 && j <= w) : !mask[i * ncol + j];
-          if (upd) ORC_TILE(X, i, j) += ORC_TILE(D, i, j);
-        }
+      }
+      for (int i = 0; i < nrow; ++i) {
+        float *restrict x = &ORC_TILE(X, i, 0);
+        const float *restrict dd = &ORC_TILE(D, i, 0);
+        const int32_t *restrict u = &ORC_TILE(U, i, 0);
+        for (int j = 0; j < ncp; ++j) x[j] = orc_sel(u[j], x[j] + dd[j], x[j]);
+      }
     }
     for (int i = 1; i <= h; ++i)
       for (int j = 1; j <= w; ++j) L[(r0 - 1 + i) * W + (c0 - 1 + j)] = ORC_TILE(X, i, j);
   }
-  free(X); free(D);
+  free(X); free(D); free(ufree); free(ufin);
 }
 
 void orc_diffuse_f64(double *fld, int H, int W, const int32_t roi[5], const uint8_t *mask,

@@ -1,8 +1,8 @@
 """The allocation-free entry point, emt6_simulate_noalloc.
 
-It exists for callers that cannot call cudaMalloc themselves (code running
-under CUDA stream capture, or inside a framework whose allocator owns all
-device memory): they pass device buffers they already own and the library
+It exists for callers that cannot call cudaMalloc themselves (code inside a
+host application or framework whose allocator owns all device memory): they
+pass device buffers they already own and the library
 keeps the working state in a fixed 8 MiB device array.  This file is
 collected last so that a failure here does not hide the other tests; it must
 pass alone in a fresh process as well as after them.
