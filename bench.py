@@ -6,23 +6,33 @@ Workload (GA-scale uniform batch): 20 seeded disc tumours (radius 6-14 on the
 30-min grid in the first 48 h) x 20 replicates = 40,000 simulations, default
 parameters, 6-s steps.  One bench step advances every simulation by
 --sim-steps steps (default 600 = one simulated hour), continuing from the
-previous bench step.  Metric: site-updates/s = simulations x steps x 2601
-interior sites / time.
+previous bench step, so the timed window is steps W*600 .. (W+K)*600 of the
+144,000-step (10-day) horizon.  Metric: site-updates/s = simulations x steps
+x 2601 interior sites / time.
 
-  value          device time (CUDA events on the batch's stream) of the
-                 step kernels, state resident in HBM (7 GB >> 129 MB L2, so
-                 every launch streams its state from HBM; no flush needed)
-  e2e            the same through the public API (emt6ro.simulation
-                 .Experiment): per step add_irradiations (doses of that hour
-                 uploaded from the host), run, get_results (counts to host)
-  roofline       FP32 algorithmic flops of the dominant (narrow-region) step
-                 kernel against the device's measured FP32 FMA rate
-  cpu_baseline   the oracle port of the reference CPU path on the host cores,
-                 on a 64-simulation sample of the same workload
+  value            device time (CUDA events on the batch's stream) of the
+                   step kernels, state resident in HBM (7 GB >> 129 MB L2, so
+                   every launch streams its state from HBM; no flush needed)
+  e2e              the same through the public API (emt6ro.simulation
+                   .Experiment): per step add_irradiations (doses of that hour
+                   uploaded from the host), run, get_results (counts to host)
+  roofline         FP32 algorithmic flops of the step kernels against the
+                   device's measured FP32 FMA rate
+  full_horizon     a stratified 4,864-simulation subset of the same batch run
+                   over all 144,000 steps, per 14,400-step (1-day) window and
+                   overall: the early-window value beside the 10-day figure
+  ref_cuda_window  this project's kernels on the window the reference arm
+                   times the reference's own CUDA kernels on (all 40,000
+                   simulations from their initial states, steps 1,800-7,800)
+  cpu_baseline     the oracle port of the reference CPU path (timing-only
+                   build: -O3, FP contraction, CPU tuning) on all host cores,
+                   a stratified 64-simulation sample over the same window,
+                   and 16 simulations over the full horizon
 
---impl reference times that CPU path (all host threads) and, where its cubin
-was built, the reference's own CUDA kernels on the same 40,000 simulations
-("ref_cuda").
+--impl reference times that CPU path (all host threads) on the same window
+and, where its cubin was built, the reference's own CUDA kernels on all
+40,000 simulations over steps 1,800-7,800 ("ref_cuda"; the reference kernels'
+fixed buffers were checked to hold this workload for 8,192 steps).
 Under torchrun (--gpus N) every rank runs its own 40,000-simulation shard
 (weak scaling); the time is the max over ranks.
 """
@@ -53,13 +63,16 @@ FLOP_PER_SITE_SUBSTEP = 33  # 3 fields x 11 flop (9-point stencil + update)
 SURROGATE_FLOP_ROW = 2 * (128 * 512 + 2 * 512 * 512 + 512) + 2 * (2 * 512 * 512) + \
     2 * (512 * 128 + 2 * 512 * 512)
 BYTES_PER_SITE_SUBSTEP = 24  # 3 fields x (4 B read + 4 B write)
+HORIZON = 144_000            # 10 days of 6-s steps
+# the reference-CUDA comparison window: 3 untimed then 10 timed 600-step
+# bench steps from the initial states (steps 1,800-7,800), inside the 8,192
+# steps checked to keep the reference kernels' fixed buffers from overflowing
+REF_WINDOW = (3, 10, 600)
+FULL_HORIZON_SIMS = 4864
+FULL_HORIZON_WINDOW = 14_400  # one simulated day
 
 
-def shard_range(total: int, rank: int, world: int):
-    """Contiguous slice [lo, hi) of `total` units for `rank` of `world`."""
-    base, extra = divmod(total, world)
-    lo = rank * base + min(rank, extra)
-    return lo, lo + base + (1 if rank < extra else 0)
+from emt6ro.ga_model.sharding import shard_range  # noqa: E402  (contiguous shard per rank)
 
 
 def large_batch(n: int = 4864):
@@ -137,16 +150,23 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+def _stratified(n_total: int, n: int) -> np.ndarray:
+    return np.unique(np.linspace(0, n_total - 1, n).astype(np.int64))
+
+
 def cpu_sample(params, tumors, protocols, sim_tumor, sim_protocol, steps, warmup, sim_steps,
                n_sample=64, threads=None):
-    """The oracle port of the reference CPU path on a sample of the workload;
-    returns (site-updates/s per timed step list, threads)."""
+    """The oracle port of the reference CPU path (its timing-only build:
+    oracle.build.fast_flags()) on a stratified sample of the workload, over
+    the same step window as the GPU: `warmup` untimed then `steps` timed
+    bench steps of `sim_steps` steps, all host threads, one simulation per
+    thread at a time.  Returns (site-updates/s per timed step, threads, n)."""
     from oracle import pyoracle as po
     from emt6ro import workloads as wl
     threads = threads or os.cpu_count() or 1
-    idx = np.linspace(0, len(sim_tumor) - 1, n_sample).astype(int)
+    idx = _stratified(len(sim_tumor), n_sample)
     doses = wl.protocol_doses(protocols, 480)
-    b = po.Batch(po.params_copy(params.native), n_sample, seed=1)
+    b = po.Batch(po.params_copy(params.native), len(idx), seed=1, lib=po.oracle_fast())
     for k, i in enumerate(idx):
         b.set(k, tumors[sim_tumor[i]].sites, doses[sim_protocol[i]], sim_index=int(i))
     for _ in range(warmup):
@@ -155,26 +175,46 @@ def cpu_sample(params, tumors, protocols, sim_tumor, sim_protocol, steps, warmup
     for _ in range(steps):
         t = time.perf_counter()
         b.run(sim_steps, nthreads=threads)
-        rates.append(n_sample * sim_steps * SITES / (time.perf_counter() - t))
-    return rates, threads, n_sample
+        rates.append(len(idx) * sim_steps * SITES / (time.perf_counter() - t))
+    return rates, threads, len(idx)
 
 
-def ref_cuda_sample(params, tumors, protocols, sim_tumor, sim_protocol, steps, warmup,
-                    sim_steps):
+def cpu_full_horizon(params, tumors, protocols, sim_tumor, sim_protocol, threads=None):
+    """The same CPU path on one stratified simulation per host thread over all
+    144,000 steps: site-updates/s over the 10-day horizon."""
+    from oracle import pyoracle as po
+    from emt6ro import workloads as wl
+    threads = threads or os.cpu_count() or 1
+    idx = _stratified(len(sim_tumor), threads)
+    doses = wl.protocol_doses(protocols, 480)
+    b = po.Batch(po.params_copy(params.native), len(idx), seed=1, lib=po.oracle_fast())
+    for k, i in enumerate(idx):
+        b.set(k, tumors[sim_tumor[i]].sites, doses[sim_protocol[i]], sim_index=int(i))
+    t = time.perf_counter()
+    b.run(HORIZON, nthreads=threads)
+    return len(idx) * HORIZON * SITES / (time.perf_counter() - t), len(idx)
+
+
+def _cpu_kind():
+    from oracle import build as ob
+    return (f"oracle/emt6_oracle.c restatement of the reference CPU path, timing-only build "
+            f"(gcc {' '.join(ob.fast_flags())}), pthreads over all host cores, one simulation "
+            "per thread at a time")
+
+
+def ref_cuda_sample(params, tumors, protocols, sim_tumor, sim_protocol):
     """The reference's own CUDA kernels (compiled from its sources for sm_103a,
     oracle/_ref/emt6ro_ref_sm103a.cubin) on the whole 40,000-simulation batch,
-    launched in the order of its Simulation::step, timed with CUDA events on
-    its stream over the same bench-step window as this project's kernels.
-    Returns a dict, or None when the cubin is absent."""
+    launched in the order of its Simulation::step and timed with CUDA events
+    on its stream over REF_WINDOW (steps 1,800-7,800 from the initial states,
+    whatever --steps/--warmup say).  Returns a dict, or None when the cubin
+    is absent."""
     from oracle import pyrefgpu
     from emt6ro import workloads as wl
     if not pyrefgpu.available():
         return None
     import torch
-    total = (warmup + steps) * sim_steps
-    if total > 8192:
-        return {"unavailable": f"{total} steps exceed the 8192 checked to stay inside the "
-                               "reference's fixed buffers for this workload"}
+    warmup, steps, sim_steps = REF_WINDOW
     doses = wl.protocol_doses(protocols, 480)
     ref = pyrefgpu.RefGpuSimulation(params, tumors, doses, sim_tumor, sim_protocol, seed=1)
     stream = torch.cuda.ExternalStream(ref.stream)
@@ -192,11 +232,15 @@ def ref_cuda_sample(params, tumors, protocols, sim_tumor, sim_protocol, steps, w
     counts = ref.counts()
     ref.close()
     n = len(sim_tumor)
+    lo, hi = warmup * sim_steps, (warmup + steps) * sim_steps
     return {"value": n * sim_steps * SITES / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms,
-            "steps": steps, "warmup": warmup, "mean_count": float(counts.mean()),
+            "steps": steps, "warmup": warmup, "sim_steps_per_step": sim_steps,
+            "mean_count": float(counts.mean()),
             "kind": "reference CUDA kernels built from its sources (nvcc 13, sm_103a, -O3), "
                     "host loop restating Simulation::step",
-            "sample": f"all {n} simulations, steps {warmup * sim_steps}-{total}"}
+            "sample": f"all {n} simulations, steps {lo}-{hi} from the initial states",
+            "compare_with": "ref_cuda_window in this project's bench line: its kernels on the "
+                            "same simulations, inputs and steps"}
 
 
 def run_reference(args, rank, world):
@@ -205,24 +249,25 @@ def run_reference(args, rank, world):
     params, tumors, protocols, st, sp = ga_batch()
     ref_cuda = None
     if not args.no_ref_cuda:
-        ref_cuda = ref_cuda_sample(params, tumors, protocols, st, sp, args.steps, args.warmup,
-                                   args.sim_steps)
+        ref_cuda = ref_cuda_sample(params, tumors, protocols, st, sp)
     rates, threads, n = cpu_sample(params, tumors, protocols, st, sp, args.steps, args.warmup,
                                    args.sim_steps)
     v = statistics.median(rates)
     ms = n * args.sim_steps * SITES / v * 1e3
+    lo, hi = args.warmup * args.sim_steps, (args.warmup + args.steps) * args.sim_steps
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded disc tumours and protocols)",
         "config": {"workload": "GA batch 20 tumours x 100 protocols x 20 runs, 53x53, 6-s "
-                               f"steps; CPU sample of {n} simulations x {args.sim_steps} steps",
+                               f"steps {lo:,}-{hi:,} of the {HORIZON:,}-step horizon; CPU "
+                               f"sample of {n} simulations",
                    "sim_steps_per_step": args.sim_steps},
         "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
-                         "sample": f"{n} of the 40,000 simulations, {args.sim_steps} steps per "
-                                   "bench step, oracle/emt6_oracle.c restatement of the "
-                                   "reference CPU path, one simulation per thread"},
+                         "sample": f"{n} of the 40,000 simulations (stratified), steps "
+                                   f"{lo:,}-{hi:,}, {args.sim_steps} steps per bench step; "
+                                   + _cpu_kind()},
         "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if ref_cuda is not None:
@@ -260,6 +305,65 @@ def _e2e(args, params, tumors, protocols, dev, seed, world, dist, bins):
     d2h = int(res.size) * 4             # living counts per get_results
     del exp
     return value, h2d, d2h
+
+
+def _ours_on_ref_window(params, tumors, protocols, st, sp, dev, seed):
+    """This project's kernels on REF_WINDOW: all simulations from their initial
+    states, 3 untimed then 10 timed 600-step bench steps (steps 1,800-7,800),
+    CUDA events on the batch's stream."""
+    import torch
+    from emt6ro.batch import Batch
+    warmup, steps, sim_steps = REF_WINDOW
+    b = Batch(params, tumors, protocols, st, sp, device=dev, seed=seed)
+    b.set_schedule(0, sim_steps)
+    stream = torch.cuda.ExternalStream(b.stream())
+    for _ in range(warmup):
+        b.run(sim_steps)
+    b.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for k in range(steps):
+        ev[k][0].record(stream)
+        b.run(sim_steps)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    b.sync()
+    ms = sum(a.elapsed_time(e) for a, e in ev) / steps
+    lo, hi = warmup * sim_steps, (warmup + steps) * sim_steps
+    return {"value": len(st) * sim_steps * SITES / (ms * 1e-3), "unit": METRIC,
+            "ms_per_step": ms, "mean_count": float(b.counts().mean()),
+            "sample": f"all {len(st)} simulations, steps {lo}-{hi} from the initial states",
+            "compare_with": "ref_cuda in the --impl reference line (the reference's own CUDA "
+                            "kernels on the same simulations, inputs and steps)"}
+
+
+def _full_horizon(params, tumors, protocols, st, sp, dev, seed):
+    """A stratified FULL_HORIZON_SIMS-simulation subset of the batch over all
+    144,000 steps: site-updates/s per one-day window and over the horizon
+    (CUDA events on the batch's stream)."""
+    import torch
+    from emt6ro.batch import Batch
+    idx = _stratified(len(st), FULL_HORIZON_SIMS)
+    b = Batch(params, tumors, protocols, st[idx], sp[idx], device=dev, seed=seed)
+    b.set_schedule(0, 1200)
+    stream = torch.cuda.ExternalStream(b.stream())
+    nwin = HORIZON // FULL_HORIZON_WINDOW
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(nwin + 1)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for k in range(nwin):
+        b.run(FULL_HORIZON_WINDOW)
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    b.sync()
+    win_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(nwin)]
+    n = len(idx)
+    per_win = [n * FULL_HORIZON_WINDOW * SITES / (ms * 1e-3) for ms in win_ms]
+    return {"value": n * HORIZON * SITES / (sum(win_ms) * 1e-3), "unit": METRIC,
+            "seconds": sum(win_ms) * 1e-3, "per_day": per_win,
+            "mean_count_day10": float(b.counts().mean()),
+            "sample": f"{n} of the {len(st)} simulations (stratified), steps 0-{HORIZON}, "
+                      "1200-step launches"}
 
 
 def run_ours(args, rank, world, dist):
@@ -319,6 +423,12 @@ def run_ours(args, rank, world, dist):
     if not args.no_e2e and not args.sims and args.workload == "ga":
         e2e_value, h2d, d2h = _e2e(args, params, tumors, protocols, dev, seed, world, dist, bins)
 
+    # ---- the reference-CUDA window and the 10-day horizon (one GPU only) -----
+    extras = args.workload == "ga" and not args.sims and world == 1 and not args.no_extras
+    ref_window = _ours_on_ref_window(params, tumors, protocols, st, sp, dev, seed + 1) \
+        if extras else None
+    full = _full_horizon(params, tumors, protocols, st, sp, dev, seed + 2) if extras else None
+
     # ---- roofline of the dominant kernel -------------------------------------
     peak = ctypes.c_double()
     N.check(N.lib().emt6_probe_fp32_peak(dev, ctypes.byref(peak)))
@@ -354,7 +464,10 @@ def run_ours(args, rank, world, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded disc tumours and protocols, default parameters)",
         "config": {"workload": ("GA batch: 20 tumours x 100 protocols x 20 runs = 40,000 "
-                                "simulations per GPU, 53x53 lattice, 6-s steps")
+                                "simulations per GPU, 53x53 lattice, 6-s steps "
+                                f"{args.warmup * args.sim_steps:,}-"
+                                f"{(args.warmup + args.steps) * args.sim_steps:,} of the "
+                                f"{HORIZON:,}-step horizon")
                                if args.workload == "ga" else
                                (f"large tumours: {B} simulations of the ragged batch's disc "
                                 "radius >= 15 tumours (wide kernel), 53x53 lattice, 6-s steps"),
@@ -370,6 +483,8 @@ def run_ours(args, rank, world, dist):
         "roofline_hbm": roof_hbm,
         "diffused_site_substeps_per_step": diffused // args.steps,
         "mean_count": mean_count,
+        "ref_cuda_window": ref_window,
+        "full_horizon": full,
     }
 
 
@@ -633,6 +748,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end API timing")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the reference-CUDA window and the 10-day horizon figures")
     ap.add_argument("--sims", type=int, default=0,
                     help="time a stratified subset of this many simulations (small "
                          "profiling case; implies --no-e2e)")
@@ -682,13 +799,19 @@ def main():
         if rank == 0 and not args.no_cpu_baseline:
             params, tumors, protocols, st, sp = (large_batch() if args.workload == "large"
                                                  else ga_batch())
-            rates, threads, n = cpu_sample(params, tumors, protocols, st, sp, 2, 1,
-                                           args.sim_steps)
+            rates, threads, n = cpu_sample(params, tumors, protocols, st, sp, args.steps,
+                                           args.warmup, args.sim_steps)
+            lo, hi = args.warmup * args.sim_steps, (args.warmup + args.steps) * args.sim_steps
             line["cpu_baseline"] = {
                 "value": statistics.median(rates), "unit": METRIC, "cores": threads,
                 "kind": "port",
-                "sample": f"{n} of the {len(st):,} simulations x {args.sim_steps} steps, "
-                          "oracle/emt6_oracle.c restatement of the reference CPU path"}
+                "sample": f"{n} of the {len(st):,} simulations (stratified), steps "
+                          f"{lo:,}-{hi:,} (the GPU's window); " + _cpu_kind()}
+            if line.get("full_horizon"):
+                v, nf = cpu_full_horizon(params, tumors, protocols, st, sp, threads)
+                line["cpu_baseline"]["full_horizon"] = {
+                    "value": v, "unit": METRIC,
+                    "sample": f"{nf} simulations (stratified), steps 0-{HORIZON:,}"}
     if rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
     if dist:

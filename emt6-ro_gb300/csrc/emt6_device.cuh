@@ -39,6 +39,7 @@ struct KParams {
   int nfree;                  // substeps over free sites before the final ROI pass
   uint32_t seed_lo, seed_hi;
   uint32_t res, length, bins;
+  uint32_t sim_base;  // added to the simulation index of every random key
 };
 
 // ---------------------------------------------------------------------------
@@ -61,7 +62,8 @@ __device__ __forceinline__ uint4 draw(const KParams &p, uint32_t step, uint32_t 
                                       uint32_t site, uint32_t occ, uint32_t purpose,
                                       uint32_t epoch) {
   return philox4x32_10(
-      make_uint4(step, sim, (site & 0xFFFFu) | ((occ & 0xFFu) << 16) | (purpose << 24), epoch),
+      make_uint4(step, sim + p.sim_base, (site & 0xFFFFu) | ((occ & 0xFFu) << 16) | (purpose << 24),
+                 epoch),
       p.seed_lo, p.seed_hi);
 }
 

@@ -966,6 +966,22 @@ int emt6_batch_set_schedule(emt6_batch *b, int32_t mode, uint32_t steps_per_laun
   return EMT6_OK;
 }
 
+int emt6_batch_set_index_base(emt6_batch *b, uint32_t base) {
+  if (!b) return fail(EMT6_ERR_INVALID, "null handle");
+  std::lock_guard<std::mutex> lk(b->mu);
+  if ((uint64_t)base + (uint64_t)b->n > 0x100000000ull)
+    return fail(EMT6_ERR_INVALID, "simulation index base + n_sims exceeds 2^32");
+  DeviceGuard g(b->device);
+  // a captured launch sequence holds the old parameters: drop it
+  EMT6_CUDA(cudaStreamSynchronize(b->stream));
+  if (b->graph_exec) {
+    cudaGraphExecDestroy(b->graph_exec);
+    b->graph_exec = nullptr;
+  }
+  b->kp.sim_base = base;
+  return EMT6_OK;
+}
+
 // ---- experiment ------------------------------------------------------------------------
 int emt6_experiment_create(const emt6_params *p, const emt6_site *tumors, int32_t n_tumors,
                            int32_t height, int32_t width, int32_t runs, int32_t protocols_num,

@@ -67,6 +67,10 @@ struct EpiArgs {
   __nv_bfloat16 *w_bf, *w_bf_t; // ADAM: BF16 W [M][N] and W^T [N][M]
   float lr, beta1, beta2, eps, bc1, bc2;
   int *err;
+  // test hook (emt6_test_mlp_gemm_timeout): when nonzero, the MMA issuer
+  // first waits this many ns on a barrier nothing arrives on, so it gives up
+  // exactly as a timed-out pipeline wait would
+  uint32_t stall_ns;
 };
 
 // ---- PTX wrappers ----------------------------------------------------------
@@ -102,14 +106,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase of `parity` to complete.  Gives up after
-// kWaitLimitNs, or early when another thread of the CTA raised `abort`.
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile int *abort) {
+// limit_ns (default kWaitLimitNs), or early when another thread of the CTA
+// raised `abort`.
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile int *abort,
+                          uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
     if (abort && *abort) return false;
-    if (global_ns() - t0 > kWaitLimitNs) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 
@@ -284,11 +290,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                                               ~static_cast<uintptr_t>(1023));
   uint8_t *sA = smem;
   uint8_t *sB = smem + STAGES * TILE_BYTES;
+  // barriers: full[STAGES], empty[STAGES], done, never (nothing arrives on
+  // it: the target of the test hook's stalled wait)
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * STAGES * TILE_BYTES);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 1);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 2);
   volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES),
-                 done = smem_u32(bars + 2 * STAGES);
+                 done = smem_u32(bars + 2 * STAGES), never = smem_u32(bars + 2 * STAGES + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   const int kb0 = blockIdx.z * nk;
@@ -300,6 +308,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       mbar_init(empty0 + 8 * s, 1);
     }
     mbar_init(done, 1);
+    mbar_init(never, 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
@@ -313,13 +322,14 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   pdl_wait();  // operands and epilogue inputs come from the previous kernel
 
   bool failed = false;
+  int issued = 0;  // k-blocks whose loads thread 0 issued
   if (threadIdx.x == 0) {
     // TMA producer
-    int issued = 0;
     for (int kb = 0; kb < nk; ++kb) {
       const int s = kb % STAGES;
       if (kb >= STAGES && !mbar_wait(empty0 + 8 * s, ((kb / STAGES) - 1) & 1, abort)) {
         failed = true;
+        *abort = 1;
         break;
       }
       mbar_expect_tx(full0 + 8 * s, 2 * TILE_BYTES);
@@ -327,19 +337,19 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       tma_load_2d(smem_u32(sB + s * TILE_BYTES), &tmB, full0 + 8 * s, (kb0 + kb) * BK, n0);
       ++issued;
     }
-    if (failed) {
-      *abort = 1;
-      // let the loads still in flight land before the CTA can exit
-      for (int kb = issued - STAGES < 0 ? 0 : issued - STAGES; kb < issued; ++kb)
-        mbar_wait(full0 + 8 * (kb % STAGES), (kb / STAGES) & 1, nullptr);
-    }
   } else if (threadIdx.x == 32) {
     // MMA issuer
-    for (int kb = 0; kb < nk; ++kb) {
+    if (ep.stall_ns && !mbar_wait(never, 0, abort, ep.stall_ns)) {
+      failed = true;
+      *abort = 1;
+      __threadfence_block();
+    }
+    for (int kb = 0; kb < nk && !failed; ++kb) {
       const int s = kb % STAGES;
       if (!mbar_wait(full0 + 8 * s, (kb / STAGES) & 1, abort)) {
         failed = true;
         *abort = 1;
+        __threadfence_block();
         break;
       }
       tc_fence_after();
@@ -355,6 +365,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   }
   __syncwarp();
   bool have = mbar_wait(done, 0, nullptr);
+  if (threadIdx.x == 0 && *abort) {
+    // a pipeline wait gave up: let the loads still in flight (at most the
+    // last STAGES issued; older stages were consumed before being reused)
+    // land before the CTA frees its shared memory
+    for (int kb = issued - STAGES < 0 ? 0 : issued - STAGES; kb < issued; ++kb)
+      mbar_wait(full0 + 8 * (kb % STAGES), (kb / STAGES) & 1, nullptr);
+  }
   have = __all_sync(0xffffffffu, have && !*abort && !failed);
   tc_fence_after();
   if (have) {
@@ -1097,6 +1114,40 @@ int emt6_test_mlp_gemm(const void *d_a, const void *d_b, float *d_c, int M, int 
   cudaFreeAsync(err, st);
   if (e != cudaSuccess) return cuda_fail(e, "emt6_test_mlp_gemm");
   if (h) return fail("emt6_test_mlp_gemm: a tensor-core pipeline wait timed out");
+  return EMT6_OK;
+}
+
+int emt6_test_mlp_gemm_timeout(const void *d_a, const void *d_b, float *d_c, int M, int N,
+                               int K, uint32_t stall_us, void *stream) {
+  if (!d_a || !d_b || !d_c || stall_us == 0 || stall_us > 100000)
+    return fail("emt6_test_mlp_gemm_timeout: null argument or stall outside 1..100000 us",
+                EMT6_ERR_INVALID);
+  if (M <= 0 || N <= 0 || K <= 0 || M % BM || N % BN || K % BK)
+    return fail("emt6_test_mlp_gemm_timeout: M, N multiples of 128 and K of 64 required",
+                EMT6_ERR_INVALID);
+  if (!encode_fn()) return fail("cuTensorMapEncodeTiled unavailable");
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, d_a, M, K) || !make_map(&mb, d_b, N, K))
+    return fail("emt6_test_mlp_gemm_timeout: cuTensorMapEncodeTiled failed");
+  int *err = nullptr;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMallocAsync(&err, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(e, "emt6_test_mlp_gemm_timeout");
+  EpiArgs ep;
+  std::memset(&ep, 0, sizeof(ep));
+  ep.M = M;
+  ep.N = N;
+  ep.c_out = d_c;
+  ep.err = err;
+  ep.stall_ns = stall_us * 1000u;
+  e = launch_gemm<EPI_STORE_F32>(ma, mb, M, N, K, ep, st);
+  int h = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(err, st);
+  if (e != cudaSuccess) return cuda_fail(e, "emt6_test_mlp_gemm_timeout");
+  if (h) return fail("emt6_test_mlp_gemm_timeout: a tensor-core pipeline wait timed out");
   return EMT6_OK;
 }
 

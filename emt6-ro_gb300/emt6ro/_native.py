@@ -16,8 +16,12 @@ _PKG = Path(__file__).resolve().parent
 _LIB_PATH = _PKG / "_lib" / "libemt6ro_gb300.so"
 
 EMT6_OK = 0
+EMT6_ERR_INVALID = 1
+EMT6_ERR_CUDA = 2
 EMT6_ERR_STATE = 3
+EMT6_ERR_IO = 4
 EMT6_ERR_LIMIT = 5
+EMT6_ERR_DEVICE = 6
 MAX_INTERIOR_HEIGHT = 54
 MAX_INTERIOR_WIDTH = 60
 INSTR_HIST_N = 300
@@ -85,6 +89,7 @@ _SIGNATURES = {
     "emt6_batch_stream": (_VP, [_VP]),
     "emt6_batch_diffused": (_c.c_int, [_VP, _P(_c.c_ulonglong)]),
     "emt6_batch_set_schedule": (_c.c_int, [_VP, _c.c_int32, _c.c_uint32]),
+    "emt6_batch_set_index_base": (_c.c_int, [_VP, _c.c_uint32]),
     "emt6_batch_launches": (_c.c_int, [_VP, _P(_c.c_ulonglong)]),
     "emt6_probe_fp32_peak": (_c.c_int, [_c.c_int32, _P(_c.c_double)]),
     "emt6_experiment_create": (_c.c_int, [_P(Params), _VP, _c.c_int32, _c.c_int32, _c.c_int32,
@@ -128,6 +133,8 @@ _SIGNATURES = {
     "emt6_mlp_sync": (_c.c_int, [_VP]),
     "emt6_mlp_set_splitk": (_c.c_int, [_VP, _c.c_int32]),
     "emt6_test_mlp_gemm": (_c.c_int, [_VP, _VP, _VP, _c.c_int32, _c.c_int32, _c.c_int32, _VP]),
+    "emt6_test_mlp_gemm_timeout": (_c.c_int, [_VP, _VP, _VP, _c.c_int32, _c.c_int32, _c.c_int32,
+                                              _c.c_uint32, _VP]),
 }
 
 _lib = None

@@ -52,6 +52,21 @@ class Batch:
     def handle(self):
         return self._h
 
+    def add_irradiations(self, protocols):
+        """protocols[i]: (step, dose) pairs of protocol i; doses accumulate into
+        bin step // protocol_resolution (Protocol::closestDose,
+        src/emt6ro/common/protocol.h:16-18)."""
+        if len(protocols) != self.n_protocols:
+            raise RuntimeError(f"Wrong number of protocols. Expected: {self.n_protocols}")
+        idx = [i for i, prot in enumerate(protocols) for _ in prot]
+        if not idx:
+            return
+        steps = np.asarray([int(t) for prot in protocols for t, _ in prot], np.uint32)
+        doses = np.asarray([float(d) for prot in protocols for _, d in prot], np.float32)
+        a = np.asarray(idx, np.int32)
+        N.check(N.lib().emt6_batch_add_irradiations(self._h, N.ptr(a), N.ptr(steps), N.ptr(doses),
+                                                    a.size))
+
     def set_doses(self, doses: np.ndarray):
         d = np.ascontiguousarray(doses, np.float32).reshape(self.n_protocols, self.bins)
         N.check(N.lib().emt6_batch_set_doses(self._h, N.ptr(d)))
@@ -115,3 +130,8 @@ class Batch:
 
     def set_schedule(self, mode: int, steps_per_launch: int = 0):
         N.check(N.lib().emt6_batch_set_schedule(self._h, int(mode), int(steps_per_launch)))
+
+    def set_index_base(self, base: int):
+        """Key simulation i's random stream by base + i: a batch holding the
+        shard [base, base + n) of a larger set draws what the whole set would."""
+        N.check(N.lib().emt6_batch_set_index_base(self._h, int(base)))

@@ -142,6 +142,13 @@ int emt6_probe_fp32_peak(int32_t device, double *tflops);
  * chunk or epoch change).  steps_per_launch: steps per kernel launch (0 keeps
  * the current value, default 1200). */
 int emt6_batch_set_schedule(emt6_batch *b, int32_t mode, uint32_t steps_per_launch);
+/* Key the random stream of simulation i by base + i (default base 0), so a
+ * batch holding the contiguous shard [base, base + n_sims) of a larger set
+ * draws exactly what one batch of the whole set would for those simulations
+ * (sharding a GA population across GPUs without changing its results).  No
+ * reference counterpart: the reference's curand streams follow its thread
+ * layout (src/emt6ro/common/random-engine.cu:8-31). */
+int emt6_batch_set_index_base(emt6_batch *b, uint32_t base);
 
 /* ---- Experiment: protocols x tumours x runs ---------------------------------
  * Replaces the pybind11 _Experiment (python/emt6ro/simulation/backend.cc:16-136).

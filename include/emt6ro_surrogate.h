@@ -76,6 +76,13 @@ int emt6_mlp_sync(emt6_mlp *net);
  * (row-major); M, N multiples of 128, K of 64.  Waits. */
 int emt6_test_mlp_gemm(const void *d_a, const void *d_b, float *d_c, int M, int N, int K,
                        void *stream);
+/* Failure-path hook of the same GEMM (no reference counterpart): the MMA
+ * issuer first waits stall_us (1..100000) microseconds on an mbarrier nothing
+ * arrives on, gives up as a timed-out pipeline wait does, the CTA waits for
+ * the loads it issued, frees its tensor memory and returns; the call reports
+ * EMT6_ERR_DEVICE and the context stays usable. */
+int emt6_test_mlp_gemm_timeout(const void *d_a, const void *d_b, float *d_c, int M, int N,
+                               int K, uint32_t stall_us, void *stream);
 
 #ifdef __cplusplus
 }

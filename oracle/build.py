@@ -1,6 +1,11 @@
 """Build recipes for the oracle (test infrastructure only).
 
 build_oracle()  compiles oracle/emt6_oracle.c -> oracle/_build/liborc.so.
+build_oracle_fast()  compiles the same file for timing only (bench.py's CPU
+                baseline) -> oracle/_build/liborc_fast.so: -O3 with FP
+                contraction allowed and, on a Neoverse-V2 host (the GB300
+                box's Grace CPU), -mcpu=neoverse-v2.  Its results may differ
+                from the checker's in the last bits; nothing checks against it.
 build_ref()     compiles the reference's own host-side sources where they lie
                 (only when the reference checkout is present) together with
                 oracle/ref_shim.cc -> oracle/_ref/libemt6_ref.so.  It never
@@ -12,8 +17,14 @@ build_ref_cubin()  compiles the reference's CUDA sources where they lie
                 oracle/_ref/emt6ro_ref_sm103a.cubin (reference checkout only;
                 the cubin holds device code alone, so it is the same file for
                 any host architecture).
+build_ref_cell_cubin()  compiles oracle/ref_cell_kernels.cu (kernels driving the
+                reference's templated cell functions with injected draws)
+                against the reference's headers, with its cell/cell.cu,
+                nvcc defaults (FMA contraction, CUDA expf), device-linked
+                into oracle/_ref/emt6ro_ref_cell_sm103a.cubin (reference
+                checkout only; device code alone, like the cubin above).
 build_ref_gpu_driver()  compiles oracle/ref_gpu_driver.cu, the host loop that
-                launches that cubin's kernels -> oracle/_build/libref_gpu.so.
+                launches those cubins' kernels -> oracle/_build/libref_gpu.so.
 
 All are plain gcc/g++/nvcc invocations (no cmake, no reference build system).
 Every float expression is compiled with -ffp-contract=off so the oracle
@@ -35,8 +46,10 @@ REFERENCE_ROOT = Path(os.environ.get("EMT6_REFERENCE_ROOT") or HERE.parent.paren
 CUDA_INC = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
 
 ORACLE_LIB = BUILD / "liborc.so"
+ORACLE_FAST_LIB = BUILD / "liborc_fast.so"
 REF_LIB = REF_OUT / "libemt6_ref.so"
 REF_CUBIN = REF_OUT / "emt6ro_ref_sm103a.cubin"
+REF_CELL_CUBIN = REF_OUT / "emt6ro_ref_cell_sm103a.cubin"
 REF_GPU_LIB = BUILD / "libref_gpu.so"
 NVCC = str(Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "bin" / "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -68,6 +81,35 @@ def build_oracle(force: bool = False) -> Path:
               "-shared", "-o", str(tmp), str(HERE / "emt6_oracle.c"), "-lm", "-lpthread"])
         os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
+
+
+def _tuning_flags() -> list[str]:
+    """CPU tuning for the timing-only build: the Grace CPU of the GB300 machine
+    (Arm Neoverse V2, MIDR part 0xd4f) gets -mcpu=neoverse-v2; any other host
+    the compiler's generic target."""
+    if platform.machine() == "aarch64":
+        try:
+            if "0xd4f" in Path("/proc/cpuinfo").read_text():
+                return ["-mcpu=neoverse-v2"]
+        except OSError:
+            pass
+        return []
+    return _arch_flags()
+
+
+def fast_flags() -> list[str]:
+    return ["-O3", "-ffp-contract=fast", *_tuning_flags()]
+
+
+def build_oracle_fast(force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    srcs = [HERE / "emt6_oracle.c", HERE / "emt6_oracle.h"]
+    if force or _stale(ORACLE_FAST_LIB, srcs):
+        tmp = ORACLE_FAST_LIB.with_suffix(".so.tmp")
+        _run(["gcc", *fast_flags(), "-std=gnu11", "-fPIC", "-shared", "-o", str(tmp),
+              str(HERE / "emt6_oracle.c"), "-lm", "-lpthread"])
+        os.replace(tmp, ORACLE_FAST_LIB)
+    return ORACLE_FAST_LIB
 
 
 def reference_available() -> bool:
@@ -132,6 +174,28 @@ def build_ref_cubin(force: bool = False) -> Path | None:
     return REF_CUBIN
 
 
+def build_ref_cell_cubin(force: bool = False) -> Path | None:
+    """The reference's cell model driven by injected draws, device code ->
+    one linked sm_103a cubin; None when the reference is absent."""
+    if not reference_available():
+        return REF_CELL_CUBIN if REF_CELL_CUBIN.exists() else None
+    src = REFERENCE_ROOT / "src"
+    cu = [HERE / "ref_cell_kernels.cu", src / "emt6ro" / "cell" / "cell.cu"]
+    if not (force or _stale(REF_CELL_CUBIN, cu)):
+        return REF_CELL_CUBIN
+    objdir = REF_OUT / "cellcu"
+    objdir.mkdir(parents=True, exist_ok=True)
+    inc = ["-I", str(src), "-I", str(REFERENCE_ROOT / "third-party" / "json")]
+    objs = [objdir / (s.stem + ".o") for s in cu]
+    for so, o in zip(cu, objs):
+        _run([NVCC, *GENCODE, "-dc", "-O3", "-DNDEBUG", "-std=c++14", *inc, "-Xcompiler",
+              "-fPIC", "-w", str(so), "-o", str(o)])
+    tmp = REF_OUT / "emt6ro_ref_cell_sm103a.tmp.cubin"
+    _run([NVCC, *GENCODE, "-dlink", "--cubin", "-o", str(tmp), *map(str, objs)])
+    os.replace(tmp, REF_CELL_CUBIN)
+    return REF_CELL_CUBIN
+
+
 def build_ref_gpu_driver(force: bool = False) -> Path:
     """Host loop for the reference's kernels (driver API) -> oracle/_build/libref_gpu.so."""
     BUILD.mkdir(exist_ok=True)
@@ -150,6 +214,8 @@ def build_ref_gpu_driver(force: bool = False) -> Path:
 
 if __name__ == "__main__":
     print(build_oracle(force=True))
+    print(build_oracle_fast(force=True))
     print(build_ref(force=True))
     print(build_ref_cubin(force=True))
+    print(build_ref_cell_cubin(force=True))
     print(build_ref_gpu_driver(force=True))

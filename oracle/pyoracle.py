@@ -165,6 +165,18 @@ def oracle() -> _Lib:
     return _oracle
 
 
+_fast = None
+
+
+def oracle_fast() -> _Lib:
+    """The timing-only build of the oracle (bench.py's CPU baseline): same
+    source, -O3 with FP contraction and CPU tuning, results not checked."""
+    global _fast
+    if _fast is None:
+        _fast = _Lib(_build.build_oracle_fast())
+    return _fast
+
+
 def reference():
     """The reference-host-code library, or None where the reference is absent."""
     global _ref

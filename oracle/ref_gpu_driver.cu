@@ -13,6 +13,9 @@
 //                   cellSimulationKernel<<<B, 512, 128 B>>>
 // The kernel names are the Itanium manglings of the reference's signatures
 // (obtained by compiling host declarations of them against its headers).
+// refgpu_find_occupied / refgpu_find_rois / refgpu_diffuse launch one of
+// those kernels alone on the current lattices, so tests can hold the oracle's
+// restatement of each kernel to the reference's own output.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -278,6 +281,265 @@ int refgpu_counts(void *h, uint32_t *out) {
   if (!ok(r, cudaMemcpyAsync(out, r->results, r->n * 4, cudaMemcpyDeviceToHost, r->stream),
           "copy")) return -1;
   return ok(r, cudaStreamSynchronize(r->stream), "sync") ? 0 : -1;
+}
+
+// One findOccupied launch (simulation.cu:41-64) on the current lattices.
+// out: n x 1024 words per simulation, as the kernel leaves them: the count,
+// then (row, column) int16 pairs in the kernel's order.  Blocks.
+int refgpu_find_occupied(void *h, uint32_t *out) {
+  Ref *r = static_cast<Ref *>(h);
+  void *a[] = {&r->lattices, &r->occupied};
+  if (!launch(r, r->k_occ, (unsigned)r->n, 32, 1, 32 * 4, a, "findOccupied")) return -1;
+  if (!ok(r, cudaMemcpyAsync(out, r->occupied, (size_t)r->n * 1024 * 4, cudaMemcpyDeviceToHost,
+                             r->stream), "copy occupied")) return -1;
+  return ok(r, cudaStreamSynchronize(r->stream), "sync") ? 0 : -1;
+}
+
+// One findROIsKernel launch (diffusion.cu:101-108).  rois: n x 4 int16
+// (origin row, origin column, height, width); masks: n x H*W bytes, the
+// border mask of (height + 2) x (width + 2) at the start of each.  Blocks.
+int refgpu_find_rois(void *h, int16_t *rois, uint8_t *masks) {
+  Ref *r = static_cast<Ref *>(h);
+  void *a[] = {&r->rois, &r->masks, &r->lattices};
+  if (!launch(r, r->k_rois, (unsigned)r->n, 16, 16, 64, a, "findROIs")) return -1;
+  if (!ok(r, cudaMemcpyAsync(rois, r->rois, (size_t)r->n * 8, cudaMemcpyDeviceToHost, r->stream),
+          "copy rois")) return -1;
+  if (!ok(r, cudaMemcpyAsync(masks, r->masks, (size_t)r->n * r->HW, cudaMemcpyDeviceToHost,
+                             r->stream), "copy masks")) return -1;
+  return ok(r, cudaStreamSynchronize(r->stream), "sync") ? 0 : -1;
+}
+
+// One diffusionKernel launch (diffusion.cu:135-191) with the ROIs and masks
+// the last findROIsKernel left.  Blocks.
+int refgpu_diffuse(void *h) {
+  Ref *r = static_cast<Ref *>(h);
+  RDiffusion dp = {r->p.dcoeffs, r->p.dts};
+  RSubs ext = r->p.ext;
+  int16_t sub = (int16_t)(r->p.time_step / r->p.dts);
+  const unsigned diff_smem = (unsigned)(12 * (r->H + 4) * (r->W + 4));
+  void *a[] = {&r->lattices, &r->rois, &r->masks, &dp, &ext, &sub};
+  if (!launch(r, r->k_diff, (unsigned)r->n, 32, 32, diff_smem, a, "diffusion")) return -1;
+  return ok(r, cudaStreamSynchronize(r->stream), "sync") ? 0 : -1;
+}
+
+// Substrate fields of every site: n x 3 x H*W floats (cho, ox, gi planes per
+// simulation).  Blocks.
+int refgpu_get_fields(void *h, float *out) {
+  Ref *r = static_cast<Ref *>(h);
+  const size_t hw = (size_t)r->HW;
+  std::vector<RSite> host((size_t)r->n * hw);
+  if (!ok(r, cudaMemcpyAsync(host.data(), r->data, host.size() * sizeof(RSite),
+                             cudaMemcpyDeviceToHost, r->stream), "copy lattices")) return -1;
+  if (!ok(r, cudaStreamSynchronize(r->stream), "sync")) return -1;
+  for (size_t i = 0; i < (size_t)r->n; ++i)
+    for (size_t q = 0; q < hw; ++q) {
+      const RSite &x = host[i * hw + q];
+      out[(i * 3 + 0) * hw + q] = x.s.cho;
+      out[(i * 3 + 1) * hw + q] = x.s.ox;
+      out[(i * 3 + 2) * hw + q] = x.s.gi;
+    }
+  return 0;
+}
+
+}  // extern "C"
+
+// ---- the reference's cell model alone (emt6ro_ref_cell_sm103a.cubin) -------
+
+namespace {
+
+RSite to_rsite(const orc_site &s) {
+  RSite d;
+  std::memset(&d, 0, sizeof(d));
+  d.s = {s.cho, s.ox, s.gi};
+  d.tir = s.time_in_repair;
+  d.irr = s.irradiation;
+  d.delay = s.repair_delay_time;
+  d.prolif = s.proliferation_time;
+  for (int i = 0; i < 5; ++i) d.times[i] = s.cycle_times[i];
+  d.mode = s.mode;
+  d.phase = s.phase;
+  d.state = s.state;
+  return d;
+}
+
+void from_rsite(const RSite &d, orc_site *s) {
+  s->cho = d.s.cho;
+  s->ox = d.s.ox;
+  s->gi = d.s.gi;
+  s->time_in_repair = d.tir;
+  s->irradiation = d.irr;
+  s->repair_delay_time = d.delay;
+  s->proliferation_time = d.prolif;
+  for (int i = 0; i < 5; ++i) s->cycle_times[i] = d.times[i];
+  s->mode = d.mode;
+  s->phase = d.phase;
+  s->state = d.state;
+}
+
+RParams to_rparams(const orc_params *op) {
+  RParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.dims = {(int16_t)op->lattice_height, (int16_t)op->lattice_width};
+  p.time_step = op->time_step;
+  p.dcoeffs = {op->diffusion_coeffs[0], op->diffusion_coeffs[1], op->diffusion_coeffs[2]};
+  p.dts = op->diffusion_time_step;
+  for (int m = 0; m < 4; ++m)
+    p.met[m] = {op->metabolism[m][0], op->metabolism[m][1], op->metabolism[m][2]};
+  p.ext = {op->external_levels[0], op->external_levels[1], op->external_levels[2]};
+  p.death_gi = op->death_gi;
+  p.quiescence_gi = op->quiescence_gi;
+  p.death_gi_production = op->death_gi_production;
+  for (int i = 0; i < 5; ++i) {
+    p.ct[i][0] = op->cycle_times[i][0];
+    p.ct[i][1] = op->cycle_times[i][1];
+  }
+  p.dl_c = op->delay_time_coeff;
+  p.dl_e = op->delay_time_exp_coeff;
+  p.sv_c = op->survival_prob_coeff;
+  p.sv_e = op->survival_prob_exp_coeff;
+  p.rht = op->repair_half_time;
+  return p;
+}
+
+// device buffers of one call, freed on every exit path
+struct Bufs {
+  std::vector<void *> p;
+  ~Bufs() {
+    for (void *x : p) cudaFree(x);
+  }
+  template <typename T>
+  T *get(size_t bytes, const void *src, std::string *err) {
+    void *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, bytes ? bytes : 1);
+    if (e == cudaSuccess && src) e = cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      *err = cudaGetErrorString(e);
+      if (d) cudaFree(d);
+      return nullptr;
+    }
+    p.push_back(d);
+    return static_cast<T *>(d);
+  }
+};
+
+thread_local std::string g_cell_err;
+
+int cell_fail(const std::string &m) {
+  g_cell_err = m;
+  return -1;
+}
+
+bool cell_fn(const char *cubin, const char *name, CUmodule *mod, CUfunction *f) {
+  if (cudaFree(nullptr) != cudaSuccess) return cell_fail("cudaFree(0)") == 0;
+  if (cuModuleLoad(mod, cubin) != CUDA_SUCCESS) return cell_fail("cuModuleLoad") == 0;
+  if (cuModuleGetFunction(f, *mod, name) != CUDA_SUCCESS) {
+    cuModuleUnload(*mod);
+    return cell_fail(name) == 0;
+  }
+  return true;
+}
+
+int cell_launch(CUmodule mod, CUfunction f, int64_t n, void **args) {
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+  CUresult e = cuLaunchKernel(f, blocks, 1, 1, 128, 1, 1, 0, nullptr, args, nullptr);
+  if (e == CUDA_SUCCESS) e = cuCtxSynchronize();
+  if (e != CUDA_SUCCESS) {
+    cuModuleUnload(mod);
+    return cell_fail("launch");
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *refgpu_cell_error() { return g_cell_err.c_str(); }
+
+// Site::step<R> of the reference's device build on n sites with injected
+// draws (ndraw per site); sites are updated in place.  Returns 0 or -1.
+int refgpu_site_step(const char *cubin, const orc_params *op, orc_site *sites,
+                     const uint32_t *vac, const float *dose, const float *draws, int ndraw,
+                     int32_t *ready, int32_t *used, int64_t n) {
+  if (n < 1 || ndraw < 1) return cell_fail("bad sizes");
+  CUmodule mod;
+  CUfunction f;
+  if (!cell_fn(cubin, "ref_site_step_kernel", &mod, &f)) return -1;
+  std::vector<RSite> rs((size_t)n);
+  for (int64_t i = 0; i < n; ++i) rs[i] = to_rsite(sites[i]);
+  Bufs b;
+  RSite *ds = b.get<RSite>(rs.size() * sizeof(RSite), rs.data(), &g_cell_err);
+  uint32_t *dv = b.get<uint32_t>((size_t)n * 4, vac, &g_cell_err);
+  float *dd = b.get<float>((size_t)n * 4, dose, &g_cell_err);
+  float *dr = b.get<float>((size_t)n * ndraw * 4, draws, &g_cell_err);
+  int32_t *dready = b.get<int32_t>((size_t)n * 4, nullptr, &g_cell_err);
+  int32_t *dused = b.get<int32_t>((size_t)n * 4, nullptr, &g_cell_err);
+  if (!ds || !dv || !dd || !dr || !dready || !dused) {
+    cuModuleUnload(mod);
+    return -1;
+  }
+  RParams p = to_rparams(op);
+  void *args[] = {&ds, &p, &dv, &dd, &dr, &ndraw, &dready, &dused, &n};
+  if (cell_launch(mod, f, n, args)) return -1;
+  cudaMemcpy(rs.data(), ds, rs.size() * sizeof(RSite), cudaMemcpyDeviceToHost);
+  cudaMemcpy(ready, dready, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(used, dused, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  for (int64_t i = 0; i < n; ++i) from_rsite(rs[i], &sites[i]);
+  cuModuleUnload(mod);
+  return 0;
+}
+
+// divideCell<R> of the reference's device build: parents updated in place,
+// children's cells written (their substrates and state are zero).
+int refgpu_divide(const char *cubin, const orc_params *op, orc_site *parents, const float *z,
+                  orc_site *children, int64_t n) {
+  if (n < 1) return cell_fail("bad sizes");
+  CUmodule mod;
+  CUfunction f;
+  if (!cell_fn(cubin, "ref_divide_kernel", &mod, &f)) return -1;
+  std::vector<RSite> rp((size_t)n), rc((size_t)n);
+  for (int64_t i = 0; i < n; ++i) rp[i] = to_rsite(parents[i]);
+  std::memset(rc.data(), 0, rc.size() * sizeof(RSite));
+  Bufs b;
+  RSite *dp = b.get<RSite>(rp.size() * sizeof(RSite), rp.data(), &g_cell_err);
+  RSite *dc = b.get<RSite>(rc.size() * sizeof(RSite), rc.data(), &g_cell_err);
+  float *dz = b.get<float>((size_t)n * 5 * 4, z, &g_cell_err);
+  if (!dp || !dc || !dz) {
+    cuModuleUnload(mod);
+    return -1;
+  }
+  RParams p = to_rparams(op);
+  void *args[] = {&dp, &dc, &p, &dz, &n};
+  if (cell_launch(mod, f, n, args)) return -1;
+  cudaMemcpy(rp.data(), dp, rp.size() * sizeof(RSite), cudaMemcpyDeviceToHost);
+  cudaMemcpy(rc.data(), dc, rc.size() * sizeof(RSite), cudaMemcpyDeviceToHost);
+  for (int64_t i = 0; i < n; ++i) {
+    from_rsite(rp[i], &parents[i]);
+    std::memset(&children[i], 0, sizeof(orc_site));
+    from_rsite(rc[i], &children[i]);
+  }
+  cuModuleUnload(mod);
+  return 0;
+}
+
+// chooseNeighbour<R> of the reference's device build for site (r, c).
+int refgpu_choose(const char *cubin, const float *u, int r, int c, int32_t *rc, int64_t n) {
+  if (n < 1) return cell_fail("bad sizes");
+  CUmodule mod;
+  CUfunction f;
+  if (!cell_fn(cubin, "ref_choose_kernel", &mod, &f)) return -1;
+  Bufs b;
+  float *du = b.get<float>((size_t)n * 4, u, &g_cell_err);
+  int32_t *drc = b.get<int32_t>((size_t)n * 8, nullptr, &g_cell_err);
+  if (!du || !drc) {
+    cuModuleUnload(mod);
+    return -1;
+  }
+  void *args[] = {&du, &r, &c, &drc, &n};
+  if (cell_launch(mod, f, n, args)) return -1;
+  cudaMemcpy(rc, drc, (size_t)n * 8, cudaMemcpyDeviceToHost);
+  cuModuleUnload(mod);
+  return 0;
 }
 
 void refgpu_destroy(void *h) {

@@ -121,6 +121,38 @@ def test_ga_model_predict(setup):
     assert f2.shape == (3,)
 
 
+def test_ga_model_fitness_equals_reference_flow_and_ignores_sharding(setup):
+    """EMT6RoModel's persistent sharded batches give, for a fixed seed, exactly
+    the fitness of the reference's flow on one GPU (one Experiment per GPU:
+    add_irradiations, run, get_results, 1500 - mean, reset;
+    python/emt6ro/ga_model/model.py:36-54) over two generations, and the same
+    fitness whether the population is one shard or split into two or three
+    (random streams keyed by the global simulation index)."""
+    import emt6ro.simulation as sim
+    from emt6ro.ga_model import EMT6RoModel
+    params, tumors = setup
+    gens = [[[(0, 2.5)], [(300, 1.25), (599, 1.25)], []],
+            [[(600, 4.0)], [], [(0, 1.0), (900, 3.0)]]]
+    steps, R = 6000, 6
+    e = sim.Experiment(params, tumors, R, 3, 0, steps, 300, seed=77)
+    expected = []
+    for prots in gens:
+        e.add_irradiations(prots)
+        e.run(steps)
+        res = e.get_results().reshape((1, 3, -1))
+        expected.append(1500 - res.mean(0).mean(1))
+        e.reset()
+    assert not np.array_equal(expected[0], expected[1])
+    models = [EMT6RoModel(params, tumors, 3, R, num_gpus=1, num_steps=steps, seed=77),
+              EMT6RoModel(params, tumors, 3, R // 2, num_steps=steps, seed=77, devices=[0, 0]),
+              EMT6RoModel(params, tumors, 3, R // 3, num_steps=steps, seed=77,
+                          devices=[0, 0, 0])]
+    assert [len(m.shards) for m in models] == [1, 2, 3]
+    for prots, exp in zip(gens, expected):
+        for m in models:
+            assert np.array_equal(m.predict(prots), exp)
+
+
 def test_instrumentation_counters(setup):
     import emt6ro.simulation as sim
     params, tumors = setup

@@ -35,6 +35,38 @@ def test_tcgen05_gemm_matches_float64(M, N, K):
     assert np.max(np.abs(c - ref) / scale) < 1e-5
 
 
+@pytest.mark.parametrize("K", [128, 1024])
+def test_gemm_pipeline_wait_timeout_returns_an_error_and_leaves_the_gpu_usable(K):
+    """The failure path of the bounded mbarrier waits, made to happen: the
+    test hook has the MMA issuer wait 200 us on a barrier nothing arrives on.
+    It gives up, the producer stops issuing, the CTA waits for the loads it
+    issued, frees its tensor memory and returns; the call reports
+    EMT6_ERR_DEVICE.  The same GEMM then runs normally on the same inputs
+    (with K = 128 every load is issued before the issuer gives up, with
+    K = 1024 the producer is stopped mid-way)."""
+    import torch
+    from emt6ro import _native as Nat
+    from oracle import mlp_oracle as mo
+    M = N = 256
+    rng = np.random.default_rng(K)
+    a = rng.normal(size=(M, K)).astype(np.float32)
+    b = rng.normal(size=(N, K)).astype(np.float32)
+    da = torch.from_numpy(_bf16_bits(a).view(np.int16)).cuda()
+    db = torch.from_numpy(_bf16_bits(b).view(np.int16)).cuda()
+    dc = torch.zeros((M, N), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    L = Nat.lib()
+    rc = L.emt6_test_mlp_gemm_timeout(da.data_ptr(), db.data_ptr(), dc.data_ptr(), M, N, K, 200,
+                                      None)
+    assert rc == Nat.EMT6_ERR_DEVICE
+    assert "timed out" in L.emt6_last_error().decode()
+    Nat.check(L.emt6_test_mlp_gemm(da.data_ptr(), db.data_ptr(), dc.data_ptr(), M, N, K, None))
+    c = dc.cpu().numpy().astype(np.float64)
+    ref = mo.bf16(a).astype(np.float64) @ mo.bf16(b).astype(np.float64).T
+    scale = np.abs(mo.bf16(a)).astype(np.float64) @ np.abs(mo.bf16(b)).astype(np.float64).T
+    assert np.max(np.abs(c - ref) / scale) < 1e-5
+
+
 def test_gemm_rejects_unaligned_shapes():
     from emt6ro import _native as Nat
     with pytest.raises(Nat.NativeError, match="multiples"):
