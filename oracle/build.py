@@ -3,9 +3,8 @@
 build_oracle()  compiles oracle/emt6_oracle.c -> oracle/_build/liborc.so.
 build_oracle_fast()  compiles the same file for timing only (bench.py's CPU
                 baseline) -> oracle/_build/liborc_fast.so: -O3 with FP
-                contraction allowed and, on a Neoverse-V2 host (the GB300
-                box's Grace CPU), -mcpu=neoverse-v2.  Its results may differ
-                from the checker's in the last bits; nothing checks against it.
+                contraction allowed.  Its results may differ from the
+                checker's in the last bits; nothing checks against it.
 build_ref()     compiles the reference's own host-side sources where they lie
                 (only when the reference checkout is present) together with
                 oracle/ref_shim.cc -> oracle/_ref/libemt6_ref.so.  It never
@@ -83,22 +82,12 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def _tuning_flags() -> list[str]:
-    """CPU tuning for the timing-only build: the Grace CPU of the GB300 machine
-    (Arm Neoverse V2, MIDR part 0xd4f) gets -mcpu=neoverse-v2; any other host
-    the compiler's generic target."""
-    if platform.machine() == "aarch64":
-        try:
-            if "0xd4f" in Path("/proc/cpuinfo").read_text():
-                return ["-mcpu=neoverse-v2"]
-        except OSError:
-            pass
-        return []
-    return _arch_flags()
-
-
 def fast_flags() -> list[str]:
-    return ["-O3", "-ffp-contract=fast", *_tuning_flags()]
+    """The timing-only build: -O3 with FP contraction for the compiler's
+    generic target of the host architecture (NEON on aarch64).  A
+    -mcpu=neoverse-v2 build raised SIGILL on the GB300 machine's host, so no CPU
+    tuning is applied."""
+    return ["-O3", "-ffp-contract=fast", *_arch_flags()]
 
 
 def build_oracle_fast(force: bool = False) -> Path:
