@@ -49,6 +49,7 @@ struct Misc {
   unsigned long long diffused;
   unsigned long long nfs;  // free sites of the current mask
   int narrow_ok, roff, coff;  // region fits the narrow kernel; row/column offset
+  int ring;  // 35 x 35 region with every free site in rows and columns 1..32
 };
 
 __host__ __device__ inline uint32_t align_up(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
@@ -250,20 +251,32 @@ __device__ void restore_colmask(uint64_t *colmask, const Misc *m) {
 // 32 region rows.  A 33-wide region fits when its ring columns 0 and 32 are
 // entirely fixed (an unclipped ROI): lanes then hold columns 1..32, and the
 // rotating shuffle hands lane 0 the value of column 32, which equals that of
-// column 0 (both fixed at the external level).  Likewise a 33-high region with
-// an entirely fixed first row holds rows 1..32; row 0 becomes a constant.
+// column 0 (both fixed at the external level).  Likewise a region with an
+// entirely fixed first row may hold rows 1.. only (row 0 becomes a constant):
+// required for 33 rows, and taken for regions wider than 23 columns (those
+// use the half-warp layout, whose bands it shortens when nrow % 4 == 1).
 // The rotating shuffle also hands column 0 its left neighbour and the last
 // column its right one: a column beyond the region (zero, like the ring
 // outside the tile) while the region has fewer columns than the lanes hold,
 // but the opposite ring column in a 32-wide region.  That is only right when
 // both ring columns are fixed; a clipped ROI (against the lattice edge) can
 // leave ring sites free, and such a 32-wide region goes to the wide kernel.
+// A 35 x 35 region (an unclipped ROI of distance 16) fits when every free site
+// lies in rows and columns 1..32 ("ring" mapping): the lanes hold that block,
+// whose neighbours outside it are all fixed, and the final substep of the
+// ROI's last row and column (33) runs as a separate pass (diffuse_half).
 // Called by one thread.
 __device__ void narrow_mapping(const uint64_t *colmask, Misc *m) {
   const int nrow = m->roi[2] + 2, ncol = m->roi[3] + 2;
-  int ok = 1, roff = 0, coff = 0;
+  int ok = 1, roff = 0, coff = 0, ring = 0;
+  uint64_t rows_any = 0;  // rows holding a free site
+  for (int j = 0; j < ncol && j < 64; ++j) rows_any |= colmask[j];
   if (m->roi[2] == 0 || m->roi[3] == 0) {
     ok = 1;
+  } else if (nrow == 35 && ncol == 35) {
+    ok = (rows_any & 1ull) == 0 && (rows_any >> 33) == 0 && colmask[0] == 0 &&
+         colmask[33] == 0 && colmask[34] == 0;
+    roff = coff = ring = 1;
   } else if (ncol > 33 || nrow > 33) {
     ok = 0;
   } else {
@@ -273,15 +286,16 @@ __device__ void narrow_mapping(const uint64_t *colmask, Misc *m) {
     }
     if (ncol == 32 && (colmask[0] != 0 || colmask[31] != 0)) ok = 0;
     if (nrow == 33) {
-      uint64_t first = 0;
-      for (int j = 0; j < ncol; ++j) first |= colmask[j] & 1ull;
-      if (first) ok = 0;
+      if (rows_any & 1ull) ok = 0;
+      roff = 1;
+    } else if (ncol > 23 && !(rows_any & 1ull)) {
       roff = 1;
     }
   }
   m->narrow_ok = ok;
   m->roff = roff;
   m->coff = coff;
+  m->ring = ok ? ring : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -447,12 +461,21 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
 // a shuffle across the half-warps, the two warps through shared memory with
 // the same producer/consumer barriers as diffuse_part.  Same sites, same
 // expressions as diffuse_part, so the results are bit-identical.
-template <int R>
+//
+// EDGE (the "ring" mapping of narrow_mapping, R = 8): the lanes hold rows and
+// columns 1..32 of a 35 x 35 region whose free sites all lie in that block.
+// Its left, right, top and bottom neighbours are fixed sites: the shuffles
+// that would wrap to the opposite column take the external level instead,
+// and the rows above and below are constants.  The final substep of the
+// ROI's last row and column (33), outside the block, is computed after the
+// loop from the block's last row and column as they were before that
+// substep (kept in shared memory), with the same expressions.
+template <int R, bool EDGE>
 __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t *__restrict__ colmask,
                                           float4 *__restrict__ xch, int part, int r0, int c0,
                                           int h, int w, int nrow, int ncol, int W, float ext,
                                           float ca, float cb, float cd, int nfree, int bar_id,
-                                          int roff, int coff) {
+                                          int roff, int coff, int field) {
   const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
   const int band = part * 2 + half;
   const int base = band * R + roff;  // region row of register row 0
@@ -475,6 +498,9 @@ __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t 
     top0 = fmaf(cd, th0, cb * tx0);
     top1 = fmaf(cd, th1, cb * tx1);
   }
+  // G of the row below band 3: the zero ring, or a fixed row (EDGE)
+  const float bot = EDGE ? fmaf(cd, ext + ext, cb * ext) : 0.f;
+  float *edge = reinterpret_cast<float *>(xch) + 256;  // EDGE: row 32 then column 32
   float x0[R], x1[R];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
@@ -492,11 +518,23 @@ __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t 
     const uint32_t u0 = fin ? rm0 : fm0;
     const uint32_t u1 = fin ? rm1 : fm1;
     const int par = s & 1;
+    if (EDGE && fin) {
+      // the block's last row and column before the final substep
+      if (band == 3) {
+        edge[2 * hl] = x0[R - 1];
+        edge[2 * hl + 1] = x1[R - 1];
+      }
+      if (hl == 15) {
+#pragma unroll
+        for (int i = 0; i < R; ++i) edge[32 + band * R + i] = x1[i];
+      }
+    }
     float h0[R], h1[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      h0[i] = __shfl_sync(kFull, x1[i], left) + x1[i];
-      h1[i] = x0[i] + __shfl_sync(kFull, x0[i], right);
+      const float lv = __shfl_sync(kFull, x1[i], left), rv = __shfl_sync(kFull, x0[i], right);
+      h0[i] = (EDGE && hl == 0 ? ext : lv) + x1[i];
+      h1[i] = x0[i] + (EDGE && hl == 15 ? ext : rv);
     }
     const float gf0 = fmaf(cd, h0[0], cb * x0[0]), gf1 = fmaf(cd, h1[0], cb * x1[0]);
     const float gl0 = fmaf(cd, h0[R - 1], cb * x0[R - 1]);
@@ -535,8 +573,8 @@ __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t 
     // above the first row, below the last row
     const float ab0 = band == 0 ? top0 : (half ? rc0 : pw.x);
     const float ab1 = band == 0 ? top1 : (half ? rc1 : pw.y);
-    const float be0 = band == 3 ? 0.f : (half ? pw.x : rc0);
-    const float be1 = band == 3 ? 0.f : (half ? pw.y : rc1);
+    const float be0 = band == 3 ? bot : (half ? pw.x : rc0);
+    const float be1 = band == 3 ? bot : (half ? pw.y : rc1);
     if (R == 1) {
       const float nv0 = fmaf(ca, x0[0], fmaf(cb, h0[0], ab0 + be0));
       const float nv1 = fmaf(ca, x1[0], fmaf(cb, h1[0], ab1 + be1));
@@ -560,6 +598,37 @@ __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t 
     if (gi >= 1 && gi <= h) {
       if (j0 >= 1 && j0 <= w) f[lat0 + gi * W + j0] = x0[i];
       if (j1 >= 1 && j1 <= w) f[lat0 + gi * W + j1] = x1[i];
+    }
+  }
+  if (EDGE) {
+    // final substep of the ROI's row 33 and column 33: every site there is
+    // fixed (x = ext) and so are all its neighbours outside the block;
+    // G = fmaf(cd, H, cb*x) and x' = fmaf(ca, x, fmaf(cb, H, G_up + G_down))
+    // as in the register tiles, from the block's values before the substep
+    named_barrier(13 + field, 64);
+    const float gfix = fmaf(cd, ext + ext, cb * ext);  // G of an all-fixed row
+    for (int k = part * 32 + lane; k < 65; k += 64) {
+      float nv;
+      int gi, gj;
+      if (k < 33) {  // (33, j): above it row 32 of the block, below it row 34
+        gj = k + 1;
+        gi = 33;
+        const float xl = gj >= 2 ? edge[gj - 2] : ext;
+        const float xc = gj <= 32 ? edge[gj - 1] : ext;
+        const float xr = gj <= 31 ? edge[gj] : ext;
+        const float gu = fmaf(cd, xl + xr, cb * xc);
+        nv = fmaf(ca, ext, fmaf(cb, ext + ext, gu + gfix));
+      } else {  // (i, 33): left of it column 32 of the block, right of it 34
+        gi = k - 32;
+        gj = 33;
+        const float xu = gi >= 2 ? edge[32 + gi - 2] : ext;
+        const float xc = edge[32 + gi - 1];
+        const float xd = gi <= 31 ? edge[32 + gi] : ext;
+        const float gu = fmaf(cd, xu + ext, cb * ext);
+        const float gd = fmaf(cd, xd + ext, cb * ext);
+        nv = fmaf(ca, ext, fmaf(cb, xc + ext, gu + gd));
+      }
+      f[lat0 + gi * W + gj] = nv;
     }
   }
 }
@@ -856,8 +925,14 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
         return;
       }
     }
-#define EMT6_HALF(RR) \
-  diffuse_half<RR>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf, bar, roff, coff)
+#define EMT6_HALF(RR)                                                                         \
+  diffuse_half<RR, false>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf, \
+                          bar, roff, coff, field)
+    if (m->ring) {
+      diffuse_half<8, true>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf,
+                            bar, roff, coff, field);
+      return;
+    }
     switch (R) {
       case 1: EMT6_HALF(1); break;
       case 2: EMT6_HALF(2); break;
@@ -1407,7 +1482,7 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192)
     __syncthreads();
     if (threadIdx.x == 0) {
       narrow_mapping(colmask, m);
-      if (WIDE_OK) m->roff = m->coff = 0;
+      if (WIDE_OK) m->roff = m->coff = m->ring = 0;
       *gn = (WIDE_OK || m->narrow_ok) ? 0u : 1u;
     }
     __syncthreads();

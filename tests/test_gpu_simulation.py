@@ -145,6 +145,25 @@ def test_33_wide_regions_bit_exact(params, oracle):
     _assert_same(b, ob, 6)
 
 
+def test_35_wide_regions_bit_exact(params, oracle):
+    """Unclipped ROIs of distance 16 (35 x 35 regions, every free site in
+    rows and columns 1..32) run on the narrow kernel with the ring mapping
+    (the block in registers, the final substep of the ROI's last row and
+    column as a separate pass); regions whose first row is fixed use the
+    row-shifted half-warp bands (25, 29 rows); a tumour clipped by the
+    lattice edge keeps the general layouts.  All match the oracle bit for
+    bit over launches that cross ROI updates and list rebuilds."""
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, r, seed=50 + r) for r in (11, 15, 16)]
+    tumors.append(wl.disc_tumor(params, 16, seed=57, center=(26, 16)))
+    protocols = [[(0, 1.0)], [(300, 3.0), (900, 2.0)]]
+    st = np.array([0, 1, 2, 3, 2, 1, 2], np.int32)
+    sp = np.array([0, 0, 0, 0, 1, 1, 1], np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 1500, seed=35)
+    assert (c == co).all()
+    _assert_same(b, ob, 7)
+
+
 def test_ragged_horizons_and_queue(params, oracle):
     from emt6ro import workloads as wl
     tumors = [wl.disc_tumor(params, r, seed=30 + r) for r in (2, 7, 18)]

@@ -237,6 +237,8 @@ def test_diffusion_step_parity(case, params, oracle):
     nrow, ncol, ran = _diffusion_parity(st, rng, params, oracle)
     if radius in (13, 14):
         assert 0 in ran  # 31-wide unclipped ROI: the shifted narrow mapping
+    if (nrow, ncol) == (35, 35):
+        assert 0 in ran  # distance-16 unclipped ROI: the ring mapping
 
 
 # Tumours against the lattice edge: ROIs clipped to fewer columns than rows,
