@@ -164,6 +164,21 @@ def test_35_wide_regions_bit_exact(params, oracle):
     _assert_same(b, ob, 7)
 
 
+def test_growing_and_shrinking_discs_bit_exact(params, oracle):
+    """Unclipped tumours of radius 3 to 14 whose regions change size as they
+    grow and die back after irradiation, crossing the narrow kernel's layouts
+    (eight-lane and half-warp bands, row-shifted mappings): bit-exact against
+    the oracle."""
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, r, seed=70 + r) for r in (3, 4, 7, 8, 10, 12, 14)]
+    protocols = [[(0, 2.0)], [(600, 5.0)]]
+    st = np.array([0, 1, 2, 3, 4, 5, 6, 3, 5, 6], np.int32)
+    sp = np.array([0, 0, 0, 0, 0, 0, 0, 1, 1, 1], np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 2000, seed=41)
+    assert (c == co).all()
+    _assert_same(b, ob, 10)
+
+
 def test_ragged_horizons_and_queue(params, oracle):
     from emt6ro import workloads as wl
     tumors = [wl.disc_tumor(params, r, seed=30 + r) for r in (2, 7, 18)]

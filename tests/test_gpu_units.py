@@ -241,6 +241,21 @@ def test_diffusion_step_parity(case, params, oracle):
         assert 0 in ran  # distance-16 unclipped ROI: the ring mapping
 
 
+@pytest.mark.parametrize("radius", range(0, 17))
+def test_diffusion_unclipped_discs_of_every_distance(radius, params, oracle):
+    """Full unclipped discs of every distance up to 16 (regions of 3 x 3 to
+    35 x 35 sites): bit-exact against the FP32 oracle and within 1e-5 of the
+    FP64 formula, on both kernel paths; every one of them runs on the narrow
+    kernel (the largest with the ring mapping)."""
+    rng = np.random.default_rng(300 + radius)
+    H = W = 53
+    center = (26 + int(rng.integers(-3, 4)), 26 + int(rng.integers(-3, 4)))
+    st = _random_lattice(rng, H, W, radius, center, density=1.0)
+    nrow, ncol, ran = _diffusion_parity(st, rng, params, oracle)
+    assert nrow == ncol and nrow <= 35
+    assert 0 in ran  # every unclipped disc up to distance 16 runs on the narrow kernel
+
+
 # Tumours against the lattice edge: ROIs clipped to fewer columns than rows,
 # which reach the register layouts a centred disc does not (eight-lane bands
 # of 2 columns with 3-4 rows and of 3 columns with 4 rows, the wide kernel's
