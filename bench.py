@@ -349,18 +349,24 @@ def _full_horizon(params, tumors, protocols, st, sp, dev, seed):
     stream = torch.cuda.ExternalStream(b.stream())
     nwin = HORIZON // FULL_HORIZON_WINDOW
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(nwin + 1)]
+    diffused = [b.diffused()]
     torch.cuda.synchronize()
     ev[0].record(stream)
     for k in range(nwin):
         b.run(FULL_HORIZON_WINDOW)
         ev[k + 1].record(stream)
+        diffused.append(b.diffused())  # waits for the window (outside its events)
     torch.cuda.synchronize()
     b.sync()
     win_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(nwin)]
     n = len(idx)
     per_win = [n * FULL_HORIZON_WINDOW * SITES / (ms * 1e-3) for ms in win_ms]
+    per_win_tf = [(diffused[k + 1] - diffused[k]) * FLOP_PER_SITE_SUBSTEP / (ms * 1e-3) / 1e12
+                  for k, ms in enumerate(win_ms)]
+    flops = (diffused[-1] - diffused[0]) * FLOP_PER_SITE_SUBSTEP
     return {"value": n * HORIZON * SITES / (sum(win_ms) * 1e-3), "unit": METRIC,
-            "seconds": sum(win_ms) * 1e-3, "per_day": per_win,
+            "fp32_tflops": flops / (sum(win_ms) * 1e-3) / 1e12,
+            "seconds": sum(win_ms) * 1e-3, "per_day": per_win, "per_day_fp32_tflops": per_win_tf,
             "mean_count_day10": float(b.counts().mean()),
             "sample": f"{n} of the {len(st)} simulations (stratified), steps 0-{HORIZON}, "
                       "1200-step launches"}
@@ -500,11 +506,12 @@ def run_ragged(args):
     tumors, prots, st, sp, hz = wl.ragged_batch(params, 30_000)
     hz = np.maximum((hz.astype(np.float64) * args.horizon_scale).astype(np.uint32), 1)
     t0 = time.perf_counter()
-    mode, chunk, table = autotune.tune(params, tumors, prots, st, sp, hz, sample=2432,
-                                       trial_steps=min(600, int(hz.min())))
+    mode, chunk, lay, table = autotune.tune(params, tumors, prots, st, sp, hz, sample=2432,
+                                            trial_steps=min(600, int(hz.min())))
     tune_s = time.perf_counter() - t0
     b = Batch(params, tumors, prots, st, sp, sim_horizon=hz, seed=0xC0FFEE)
     b.set_schedule(mode, chunk)
+    b.set_layouts(lay)
     stream = torch.cuda.ExternalStream(b.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(0)
@@ -529,9 +536,11 @@ def run_ragged(args):
                                "horizons 5/10/20 days mixed",
                    "horizon_scale": args.horizon_scale,
                    "horizons_steps": sorted({int(x) for x in np.unique(hz)}),
-                   "schedule_mode": mode, "steps_per_launch": chunk},
+                   "schedule_mode": mode, "steps_per_launch": chunk, "tile_shapes": lay},
         "tail_latency_s": ms * 1e-3,
-        "autotune": {"seconds": tune_s, "table": [[m, c, round(t, 4)] for m, c, t in table]},
+        "autotune": {"seconds": tune_s,
+                     "table": [[m, c, y, round(t, 4)] for m, c, y, t in table],
+                     "columns": ["schedule mode", "steps per launch", "tile shapes", "seconds"]},
         "clocks": clocks.summary(), "gpu_launches": b.launches(),
     }
 

@@ -40,7 +40,15 @@ struct KParams {
   uint32_t seed_lo, seed_hi;
   uint32_t res, length, bins;
   uint32_t sim_base;  // added to the simulation index of every random key
+  // tile shapes the step kernels may use (kLayout*); results do not depend on it
+  uint32_t layouts;
 };
+
+// kLayoutBands: eight-lane bands for narrow regions up to 23 columns;
+// kLayoutWideBands: three-column half-warp bands for 41-48-row wide regions;
+// kLayoutRing: the ring mapping of 35 x 35 regions on the narrow kernel
+constexpr uint32_t kLayoutBands = 1u, kLayoutWideBands = 2u, kLayoutRing = 4u,
+                   kLayoutAll = 7u;
 
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., SC'11), counter = (step, sim, site|occ<<16|

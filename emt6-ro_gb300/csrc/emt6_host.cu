@@ -27,6 +27,7 @@
 #include "emt6_kernels.h"
 
 using emt6::KParams;
+using emt6::kLayoutAll;
 
 namespace {
 
@@ -135,6 +136,7 @@ KParams make_kparams(const emt6_params &p, uint64_t seed, uint32_t res, uint32_t
   k.res = res;
   k.length = length;
   k.bins = bins;
+  k.layouts = kLayoutAll;
   return k;
 }
 
@@ -963,6 +965,21 @@ int emt6_batch_set_schedule(emt6_batch *b, int32_t mode, uint32_t steps_per_laun
   b->sched = mode & 1;
   b->use_graph = (mode & 2) != 0;
   if (steps_per_launch) b->chunk = steps_per_launch;
+  return EMT6_OK;
+}
+
+int emt6_batch_set_layouts(emt6_batch *b, uint32_t layouts) {
+  if (!b) return fail(EMT6_ERR_INVALID, "null handle");
+  if (layouts & ~kLayoutAll) return fail(EMT6_ERR_INVALID, "unknown layout bits");
+  std::lock_guard<std::mutex> lk(b->mu);
+  DeviceGuard g(b->device);
+  // a captured launch sequence holds the old parameters: drop it
+  EMT6_CUDA(cudaStreamSynchronize(b->stream));
+  if (b->graph_exec) {
+    cudaGraphExecDestroy(b->graph_exec);
+    b->graph_exec = nullptr;
+  }
+  b->kp.layouts = layouts;
   return EMT6_OK;
 }
 

@@ -50,6 +50,7 @@ struct Misc {
   unsigned long long nfs;  // free sites of the current mask
   int narrow_ok, roff, coff;  // region fits the narrow kernel; row/column offset
   int ring;  // 35 x 35 region with every free site in rows and columns 1..32
+  int wblk;  // 49 x 49 region with every free site in rows and columns 1..46
 };
 
 __host__ __device__ inline uint32_t align_up(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
@@ -266,14 +267,14 @@ __device__ void restore_colmask(uint64_t *colmask, const Misc *m) {
 // whose neighbours outside it are all fixed, and the final substep of the
 // ROI's last row and column (33) runs as a separate pass (diffuse_half).
 // Called by one thread.
-__device__ void narrow_mapping(const uint64_t *colmask, Misc *m) {
+__device__ void narrow_mapping(const uint64_t *colmask, Misc *m, uint32_t layouts) {
   const int nrow = m->roi[2] + 2, ncol = m->roi[3] + 2;
   int ok = 1, roff = 0, coff = 0, ring = 0;
   uint64_t rows_any = 0;  // rows holding a free site
   for (int j = 0; j < ncol && j < 64; ++j) rows_any |= colmask[j];
   if (m->roi[2] == 0 || m->roi[3] == 0) {
     ok = 1;
-  } else if (nrow == 35 && ncol == 35) {
+  } else if (nrow == 35 && ncol == 35 && (layouts & kLayoutRing)) {
     ok = (rows_any & 1ull) == 0 && (rows_any >> 33) == 0 && colmask[0] == 0 &&
          colmask[33] == 0 && colmask[34] == 0;
     roff = coff = ring = 1;
@@ -296,6 +297,13 @@ __device__ void narrow_mapping(const uint64_t *colmask, Misc *m) {
   m->roff = roff;
   m->coff = coff;
   m->ring = ok ? ring : 0;
+  // an unclipped ROI of distance 23 (49 x 49 region): the wide kernel's
+  // three-column bands hold its rows and columns 1..48 (wblk)
+  int wblk = 0;
+  if (nrow == 49 && ncol == 49 && (layouts & kLayoutWideBands) && (rows_any & 1ull) == 0 &&
+      (rows_any >> 47) == 0 && colmask[0] == 0 && colmask[47] == 0 && colmask[48] == 0)
+    wblk = 1;
+  m->wblk = wblk;
 }
 
 // ---------------------------------------------------------------------------
@@ -758,15 +766,22 @@ __device__ __noinline__ void diffuse_band(float *__restrict__ f, const uint64_t 
 // substep, as in diffuse_part.  Same sites and expressions as diffuse_part,
 // so bit-identical results, with 18 lane slots per lane (R = 6) instead of 24
 // (RH = 12).
-template <int R>
+//
+// BLK (49 x 49 regions of unclipped ROIs, whose free sites all lie in rows and
+// columns 1..46): the bands hold rows and columns 1..48 instead of 0..47, so
+// the 49th column fits; row 0 above the first band is fixed (a constant G),
+// and the wrap of column 1's left neighbour lands on column 48, which is
+// fixed like column 0.
+template <int R, bool BLK>
 __device__ __noinline__ void diffuse_wband(float *__restrict__ f, const uint64_t *__restrict__ colmask,
                                            float4 *__restrict__ xch, int part, int r0, int c0,
                                            int h, int w, int nrow, int ncol, int W, float ext,
                                            float ca, float cb, float cd, int nfree, int bar_id) {
-  constexpr int C = 3, NPW = 4;
+  constexpr int C = 3, NPW = 4, OFF = BLK ? 1 : 0;
   const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
   const int band = part * 2 + half;
-  const int base = band * R;  // region row of register row 0
+  const int base = band * R + OFF;  // region row of register row 0
+  const float top = BLK ? fmaf(cd, ext + ext, cb * ext) : 0.f;  // G of the row above band 0
   const int left = (lane & 16) | ((hl + 15) & 15), right = (lane & 16) | ((hl + 1) & 15);
   const uint32_t rowsel = (1u << R) - 1u;
   const uint32_t roirows = (uint32_t)(((((1ull << h) - 1ull) << 1)) >> base) & rowsel;
@@ -775,7 +790,7 @@ __device__ __noinline__ void diffuse_wband(float *__restrict__ f, const uint64_t
   float X[C][R];
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    const int j = C * hl + c;
+    const int j = C * hl + c + OFF;
     fm[c] = (j < ncol) ? (uint32_t)(colmask[j] >> base) & rowsel : 0u;
     rm[c] = (j >= 1 && j <= w) ? roirows : 0u;
 #pragma unroll
@@ -824,7 +839,7 @@ __device__ __noinline__ void diffuse_wband(float *__restrict__ f, const uint64_t
       const uint32_t u = fin ? rm[c] : fm[c];
       // the warp above's last row (first half-warp) or the warp below's first
       // row (second half-warp); zero beyond the field's first and last band
-      float pw = 0.f;
+      float pw = (half == 0 && part == 0) ? top : 0.f;
       if (half == 0 && part > 0) pw = slot(par, part - 1, 1)[c];
       if (half == 1 && part < NPW - 1) pw = slot(par, part + 1, 0)[c];
       const float ab = half ? rc[c] : pw;  // above the first row
@@ -857,7 +872,7 @@ __device__ __noinline__ void diffuse_wband(float *__restrict__ f, const uint64_t
   // write back the ROI interior
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    const int j = C * hl + c;
+    const int j = C * hl + c + OFF;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int gi = base + i;
@@ -904,7 +919,7 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
     const int R = (nrow - roff + 3) / 4;
     // (a band layout needs a spare lane column: the shuffle that fetches
     // column 0's left neighbour then wraps to a zero column)
-    if (roff == 0 && coff == 0 && ncol <= 23) {
+    if (roff == 0 && coff == 0 && ncol <= 23 && (p.layouts & kLayoutBands)) {
       const int R8 = (nrow + 7) / 8;  // nrow <= 32 without a row offset
       const bool two = ncol <= 15;
       if ((two ? 2 : 3) * R8 < 2 * R) {
@@ -947,13 +962,17 @@ __device__ __forceinline__ void diffuse_step(float *fld, const uint64_t *colmask
 #undef EMT6_HALF
   } else if (!WIDE_OK || ncol <= 31) {
     EMT6_CASES(false)
-  } else if (ncol <= 47 && nrow > 40 && nrow <= 48) {
+  } else if ((p.layouts & kLayoutWideBands) && ncol <= 47 && nrow > 40 && nrow <= 48) {
     // 32-47 columns (a spare lane column for the wrap of column 0's left
     // neighbour) and 41-48 rows: half-warp bands of three columns per lane
     // (6 rows each) instead of 12-row tiles of two columns per lane.  Shorter
     // bands do not pay for their per-substep exchange: measured slower than
     // the 10-row tiles at 33-40 rows.
-    diffuse_wband<6>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf, bar);
+    diffuse_wband<6, false>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf,
+                            bar);
+  } else if (m->wblk) {
+    diffuse_wband<6, true>(f, colmask, x, part, r0, c0, h, w, nrow, ncol, W, ext, ca, cb, cd, nf,
+                           bar);
   } else {
     EMT6_CASES(WIDE_OK)
   }
@@ -1106,7 +1125,7 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
       unsigned long long nf = 0;
       for (int j = 0; j < 64; ++j) nf += __popcll(colmask[j]);
       m->nfs = nf;
-      narrow_mapping(colmask, m);
+      narrow_mapping(colmask, m, p.layouts);
     }
     float4 *cells = a.cell + sim * (int64_t)HW * 3;
     const uint32_t step0 = a.step[sim];
@@ -1125,7 +1144,7 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
           unsigned long long nf = 0;
           for (int j = 0; j < 64; ++j) nf += __popcll(colmask[j]);
           m->nfs = nf;
-          narrow_mapping(colmask, m);
+          narrow_mapping(colmask, m, p.layouts);
         }
         __syncthreads();
       }
@@ -1481,8 +1500,9 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192)
     restore_colmask(colmask, m);
     __syncthreads();
     if (threadIdx.x == 0) {
-      narrow_mapping(colmask, m);
+      narrow_mapping(colmask, m, p.layouts);
       if (WIDE_OK) m->roff = m->coff = m->ring = 0;
+      if (!WIDE_OK) m->wblk = 0;
       *gn = (WIDE_OK || m->narrow_ok) ? 0u : 1u;
     }
     __syncthreads();

@@ -90,6 +90,7 @@ _SIGNATURES = {
     "emt6_batch_diffused": (_c.c_int, [_VP, _P(_c.c_ulonglong)]),
     "emt6_batch_set_schedule": (_c.c_int, [_VP, _c.c_int32, _c.c_uint32]),
     "emt6_batch_set_index_base": (_c.c_int, [_VP, _c.c_uint32]),
+    "emt6_batch_set_layouts": (_c.c_int, [_VP, _c.c_uint32]),
     "emt6_batch_launches": (_c.c_int, [_VP, _P(_c.c_ulonglong)]),
     "emt6_probe_fp32_peak": (_c.c_int, [_c.c_int32, _P(_c.c_double)]),
     "emt6_experiment_create": (_c.c_int, [_P(Params), _VP, _c.c_int32, _c.c_int32, _c.c_int32,

@@ -1,15 +1,20 @@
-"""Launch autotuner for the batch engine.
+"""Launch and tile-shape autotuner for the batch engine.
 
-A CTA holds one simulation's lattice in shared memory, and the kernels pick
-the register tiling (warps per field, rows per warp, one or two columns per
-lane) per region themselves.  What is left to tune per workload is how the
-step loop is launched: steps per launch (longer launches amortise the
-per-launch load/store of every lattice; shorter ones let simulations that
-finish or outgrow the narrow kernel be rescheduled sooner), the schedule (one
-CTA per simulation vs persistent CTAs over a device work queue ordered by
-horizon) and CUDA-graph replay of the launch sequence.  The tuner times each
-candidate on a stratified sample of the batch, from identical initial states,
-and returns the fastest.
+A CTA holds one simulation's lattice in shared memory (52 KB: an SM holds
+four whatever the grouping, so one simulation per CTA is fixed), and the
+kernels pick a register tiling per region.  Tuned per workload, in two
+stages on a stratified sample of the batch from identical initial states:
+
+1. how the step loop is launched: steps per launch (longer launches amortise
+   the per-launch load/store of every lattice; shorter ones let simulations
+   that finish or outgrow the narrow kernel be rescheduled sooner), the
+   schedule (one CTA per simulation vs persistent CTAs over a device work
+   queue ordered by horizon) and CUDA-graph replay of the launch sequence;
+2. with the fastest launch, which tile shapes the kernels may use
+   (Batch.LAYOUT_* bits: eight-lane bands for small regions, three-column
+   bands for 41-48-row wide regions, the 35 x 35 ring mapping).
+
+Every candidate gives bit-identical results; only time differs.
 """
 from __future__ import annotations
 
@@ -22,6 +27,7 @@ from .batch import Batch
 
 DEFAULT_CHUNKS = (300, 600, 1200, 2400)
 DEFAULT_MODES = (0, 1, 2, 3)  # bit 0: work queue, bit 1: CUDA graph
+DEFAULT_LAYOUTS = tuple(range(8))  # subsets of Batch.LAYOUT_* bits
 
 _cache: dict = {}
 
@@ -32,17 +38,20 @@ def _sample(n: int, k: int) -> np.ndarray:
 
 def tune(params, tumors, protocols, sim_tumor, sim_protocol, sim_horizon=None, *, device=0,
          sample=2432, trial_steps=600, warm_steps=64, chunks=DEFAULT_CHUNKS, modes=DEFAULT_MODES,
-         seed=1, key=None):
-    """Returns (mode, steps_per_launch, table) with table = [(mode, chunk, seconds)]."""
+         layouts=DEFAULT_LAYOUTS, seed=1, key=None):
+    """Returns (mode, steps_per_launch, layouts, table) with table rows
+    (mode, chunk, layouts, seconds): stage 1 with all tile shapes allowed,
+    stage 2 over `layouts` with the fastest (mode, chunk)."""
     if key is not None and key in _cache:
         return _cache[key]
     idx = _sample(len(sim_tumor), sample)
     st = np.asarray(sim_tumor)[idx]
     sp = np.asarray(sim_protocol)[idx]
     hz = None if sim_horizon is None else np.asarray(sim_horizon)[idx]
-    table = []
-    for mode, chunk in itertools.product(modes, chunks):
+
+    def trial(mode, chunk, lay):
         b = Batch(params, tumors, protocols, st, sp, sim_horizon=hz, device=device, seed=seed)
+        b.set_layouts(lay)
         b.set_schedule(mode, min(chunk, warm_steps))
         b.run(warm_steps)
         b.sync()
@@ -50,10 +59,18 @@ def tune(params, tumors, protocols, sim_tumor, sim_protocol, sim_horizon=None, *
         t0 = time.perf_counter()
         b.run(trial_steps)
         b.sync()
-        table.append((mode, chunk, time.perf_counter() - t0))
+        dt = time.perf_counter() - t0
         del b
-    mode, chunk, _ = min(table, key=lambda r: r[2])
-    res = (mode, chunk, table)
+        return dt
+
+    table = [(mode, chunk, Batch.LAYOUT_ALL, trial(mode, chunk, Batch.LAYOUT_ALL))
+             for mode, chunk in itertools.product(modes, chunks)]
+    mode, chunk, _, _ = min(table, key=lambda r: r[3])
+    for lay in layouts:
+        if lay != Batch.LAYOUT_ALL:
+            table.append((mode, chunk, lay, trial(mode, chunk, lay)))
+    mode, chunk, lay, _ = min(table, key=lambda r: r[3])
+    res = (mode, chunk, lay, table)
     if key is not None:
         _cache[key] = res
     return res

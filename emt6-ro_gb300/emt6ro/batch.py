@@ -131,6 +131,13 @@ class Batch:
     def set_schedule(self, mode: int, steps_per_launch: int = 0):
         N.check(N.lib().emt6_batch_set_schedule(self._h, int(mode), int(steps_per_launch)))
 
+    LAYOUT_BANDS, LAYOUT_WIDE_BANDS, LAYOUT_RING, LAYOUT_ALL = 1, 2, 4, 7
+
+    def set_layouts(self, layouts: int):
+        """Tile shapes the step kernels may use (LAYOUT_* bits; results do not
+        depend on it, only time)."""
+        N.check(N.lib().emt6_batch_set_layouts(self._h, int(layouts)))
+
     def set_index_base(self, base: int):
         """Key simulation i's random stream by base + i: a batch holding the
         shard [base, base + n) of a larger set draws what the whole set would."""

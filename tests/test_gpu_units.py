@@ -256,6 +256,18 @@ def test_diffusion_unclipped_discs_of_every_distance(radius, params, oracle):
     assert 0 in ran  # every unclipped disc up to distance 16 runs on the narrow kernel
 
 
+@pytest.mark.parametrize("radius", [22, 23, 24])
+def test_diffusion_large_unclipped_discs(radius, params, oracle):
+    """Unclipped discs of distance 22-24 on the wide kernel (47 x 47 regions
+    on three-column bands, 49 x 49 on the same bands shifted to rows and
+    columns 1..48, 51 x 51 on two-column tiles): bit-exact against the FP32
+    oracle and within 1e-5 of the FP64 formula."""
+    rng = np.random.default_rng(500 + radius)
+    st = _random_lattice(rng, 53, 53, radius, (26, 26), density=1.0)
+    nrow, ncol, ran = _diffusion_parity(st, rng, params, oracle)
+    assert (nrow, ncol) == (2 * radius + 3,) * 2 and ran == [1]
+
+
 # Tumours against the lattice edge: ROIs clipped to fewer columns than rows,
 # which reach the register layouts a centred disc does not (eight-lane bands
 # of 2 columns with 3-4 rows and of 3 columns with 4 rows, the wide kernel's
