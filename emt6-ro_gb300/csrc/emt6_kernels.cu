@@ -82,6 +82,19 @@ size_t run_kernel_smem(int HW, int lcap, bool wide) {
 }
 
 // ---------------------------------------------------------------------------
+// x where bit i of u is clear, nv where it is set: the fixed-site select of
+// the diffusion tiles.  Written as a bitwise blend with a mask made by
+// shifting bit i into the sign and back, so it issues a shift pair and one
+// three-input logic op instead of a bit test, a predicate and a select: the
+// ALU pipe (the busiest of the step kernels) carries less, and the result is
+// the same bits.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float sel_bit(uint32_t u, int i, float nv, float x) {
+  const uint32_t m = (uint32_t)((int32_t)(u << (31 - i)) >> 31);
+  return __uint_as_float((__float_as_uint(nv) & m) | (__float_as_uint(x) & ~m));
+}
+
+// ---------------------------------------------------------------------------
 // block reductions
 // ---------------------------------------------------------------------------
 template <int NT>
@@ -398,7 +411,7 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
           gn = gx;
         }
         const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0, gm + gn));
-        if ((u0 >> i) & 1u) x0[i] = nv0;
+        x0[i] = sel_bit(u0, i, nv0, x0[i]);
         gm = gc;
         gc = gn;
         hc0 = hn0;
@@ -439,8 +452,8 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
         }
         const float nv0 = fmaf(ca, x0[i], fmaf(cb, hc0, gm0 + gn0));
         const float nv1 = fmaf(ca, x1[i], fmaf(cb, hc1, gm1 + gn1));
-        if ((u0 >> i) & 1u) x0[i] = nv0;
-        if ((u1 >> i) & 1u) x1[i] = nv1;
+        x0[i] = sel_bit(u0, i, nv0, x0[i]);
+        x1[i] = sel_bit(u1, i, nv1, x1[i]);
         gm0 = gc0;
         gc0 = gn0;
         gm1 = gc1;
@@ -565,8 +578,8 @@ __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t 
       const float gn1 = (i + 1 == R - 1) ? gl1 : fmaf(cd, h1[i + 1], cb * x1[i + 1]);
       const float nv0 = fmaf(ca, x0[i], fmaf(cb, h0[i], gm0 + gn0));
       const float nv1 = fmaf(ca, x1[i], fmaf(cb, h1[i], gm1 + gn1));
-      if ((u0 >> i) & 1u) x0[i] = nv0;
-      if ((u1 >> i) & 1u) x1[i] = nv1;
+      x0[i] = sel_bit(u0, i, nv0, x0[i]);
+      x1[i] = sel_bit(u1, i, nv1, x1[i]);
       gm0 = gc0;
       gm1 = gc1;
       gc0 = gn0;
@@ -586,17 +599,17 @@ __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t 
     if (R == 1) {
       const float nv0 = fmaf(ca, x0[0], fmaf(cb, h0[0], ab0 + be0));
       const float nv1 = fmaf(ca, x1[0], fmaf(cb, h1[0], ab1 + be1));
-      if (u0 & 1u) x0[0] = nv0;
-      if (u1 & 1u) x1[0] = nv1;
+      x0[0] = sel_bit(u0, 0, nv0, x0[0]);
+      x1[0] = sel_bit(u1, 0, nv1, x1[0]);
     } else {
       const float f0 = fmaf(ca, x0[0], fmaf(cb, h0[0], ab0 + g_second0));
       const float f1 = fmaf(ca, x1[0], fmaf(cb, h1[0], ab1 + g_second1));
       const float l0 = fmaf(ca, x0[R - 1], fmaf(cb, h0[R - 1], g_penult0 + be0));
       const float l1 = fmaf(ca, x1[R - 1], fmaf(cb, h1[R - 1], g_penult1 + be1));
-      if (u0 & 1u) x0[0] = f0;
-      if (u1 & 1u) x1[0] = f1;
-      if ((u0 >> (R - 1)) & 1u) x0[R - 1] = l0;
-      if ((u1 >> (R - 1)) & 1u) x1[R - 1] = l1;
+      x0[0] = sel_bit(u0, 0, f0, x0[0]);
+      x1[0] = sel_bit(u1, 0, f1, x1[0]);
+      x0[R - 1] = sel_bit(u0, (R - 1), l0, x0[R - 1]);
+      x1[R - 1] = sel_bit(u1, (R - 1), l1, x1[R - 1]);
     }
   }
   // write back the ROI interior
@@ -720,7 +733,7 @@ __device__ __noinline__ void diffuse_band(float *__restrict__ f, const uint64_t 
       for (int i = 1; i < R - 1; ++i) {
         const float gn = (i + 1 == R - 1) ? gl[c] : fmaf(cd, hs[c][i + 1], cb * X[c][i + 1]);
         const float nv = fmaf(ca, X[c][i], fmaf(cb, hs[c][i], gm + gn));
-        if ((u >> i) & 1u) X[c][i] = nv;
+        X[c][i] = sel_bit(u, i, nv, X[c][i]);
         gm = gc;
         gc = gn;
       }
@@ -736,12 +749,12 @@ __device__ __noinline__ void diffuse_band(float *__restrict__ f, const uint64_t 
       const float be = band == 2 * K - 1 ? 0.f : (bw == K - 1 ? pw : dn[c]);
       if (R == 1) {
         const float nv = fmaf(ca, X[c][0], fmaf(cb, hs[c][0], ab + be));
-        if (u & 1u) X[c][0] = nv;
+        X[c][0] = sel_bit(u, 0, nv, X[c][0]);
       } else {
         const float f0 = fmaf(ca, X[c][0], fmaf(cb, hs[c][0], ab + g_second[c]));
         const float l0 = fmaf(ca, X[c][R - 1], fmaf(cb, hs[c][R - 1], g_penult[c] + be));
-        if (u & 1u) X[c][0] = f0;
-        if ((u >> (R - 1)) & 1u) X[c][R - 1] = l0;
+        X[c][0] = sel_bit(u, 0, f0, X[c][0]);
+        X[c][R - 1] = sel_bit(u, (R - 1), l0, X[c][R - 1]);
       }
     }
   }
@@ -846,7 +859,7 @@ __device__ __noinline__ void diffuse_wband(float *__restrict__ f, const uint64_t
       const float be = half ? pw : rc[c];  // below the last row
       if (R == 1) {
         const float nv = fmaf(ca, X[c][0], fmaf(cb, hs[c][0], ab + be));
-        if (u & 1u) X[c][0] = nv;
+        X[c][0] = sel_bit(u, 0, nv, X[c][0]);
       } else {
         // rows 1 .. R-2, then the first and last rows (their G taken before
         // any row of the band changes)
@@ -857,15 +870,15 @@ __device__ __noinline__ void diffuse_wband(float *__restrict__ f, const uint64_t
         for (int i = 1; i < R - 1; ++i) {
           const float gn = (i + 1 == R - 1) ? gl[c] : fmaf(cd, hs[c][i + 1], cb * X[c][i + 1]);
           const float nv = fmaf(ca, X[c][i], fmaf(cb, hs[c][i], gm + gn));
-          if ((u >> i) & 1u) X[c][i] = nv;
+          X[c][i] = sel_bit(u, i, nv, X[c][i]);
           gm = gc;
           gc = gn;
         }
         const float g_penult = R > 2 ? gm : gf[c];
         const float f0 = fmaf(ca, X[c][0], fmaf(cb, hs[c][0], ab + g_second));
         const float l0 = fmaf(ca, X[c][R - 1], fmaf(cb, hs[c][R - 1], g_penult + be));
-        if (u & 1u) X[c][0] = f0;
-        if ((u >> (R - 1)) & 1u) X[c][R - 1] = l0;
+        X[c][0] = sel_bit(u, 0, f0, X[c][0]);
+        X[c][R - 1] = sel_bit(u, (R - 1), l0, X[c][R - 1]);
       }
     }
   }
