@@ -381,6 +381,9 @@ __device__ __noinline__ void diffuse_part(float *__restrict__ f, const uint64_t 
     return reinterpret_cast<float *>(xch) +
            ((NP == 2 ? (par * 2 + pt) : ((par * NP + pt) * 2 + side)) * 32 + lane) * (WIDE ? 2 : 1);
   };
+  // two substeps per iteration: the loop-carried tile registers need no
+  // copies at the back edge of every substep
+#pragma unroll 2
   for (int s = 0; s <= nfree; ++s) {
     const bool fin = (s == nfree);
     const uint32_t u0 = fin ? rm0 : fm0;
@@ -534,6 +537,9 @@ __device__ __noinline__ void diffuse_half(float *__restrict__ f, const uint64_t 
   // its second half-warp), slot 1 = part 1's first row (its first half-warp)
   float2 *xs = reinterpret_cast<float2 *>(xch);
   const bool writes = (part == 0) ? half == 1 : half == 0;
+  // two substeps per iteration: the loop-carried tile registers need no
+  // copies at the back edge of every substep
+#pragma unroll 2
   for (int s = 0; s <= nfree; ++s) {
     const bool fin = (s == nfree);
     const uint32_t u0 = fin ? rm0 : fm0;
@@ -695,6 +701,9 @@ __device__ __noinline__ void diffuse_band(float *__restrict__ f, const uint64_t 
   // part 0's last row (its band 3) or part 1's first row (its band 0)
   float *xs = reinterpret_cast<float *>(xch);
   const bool writes = (part == 0) ? bw == K - 1 : bw == 0;
+  // two substeps per iteration: the loop-carried tile registers need no
+  // copies at the back edge of every substep
+#pragma unroll 2
   for (int s = 0; s <= nfree; ++s) {
     const bool fin = (s == nfree);
     const int par = s & 1;
@@ -818,6 +827,9 @@ __device__ __noinline__ void diffuse_wband(float *__restrict__ f, const uint64_t
   auto slot = [&](int par, int pt, int side) -> float * {
     return reinterpret_cast<float *>(xch) + (((par * NPW + pt) * 2 + side) * 16 + hl) * C;
   };
+  // two substeps per iteration: the loop-carried tile registers need no
+  // copies at the back edge of every substep
+#pragma unroll 2
   for (int s = 0; s <= nfree; ++s) {
     const bool fin = (s == nfree);
     const int par = s & 1;
