@@ -11,15 +11,18 @@ each).  The reference's own CUDA build cannot run these horizons: its
 per-thread occupied-site buffers overflow once a tumour spans more than 32
 columns (src/emt6ro/simulation/simulation.cu:46,58).  This project's
 kernels, with their own Philox stream, run 1,000 replicates of each case and
-must match in mean (2%), 10/50/90% quantiles and a two-sample
-Kolmogorov-Smirnov test (p > 0.01).
+must match in mean, 10/50/90% quantiles and a two-sample Kolmogorov-Smirnov
+test (p > 0.01).
 
 Some 10-day outcomes are multimodal (a GA protocol can leave either a
-regrown or a shrunken tumour), and a sample quantile that falls between two
-modes is uncertain by tens of cells at these sample sizes.  A quantile
-therefore matches when it is within 3% + 2 cells, or within 3.3 combined
-bootstrap standard errors of the two samples' quantiles (about a 0.1%
-two-sided level per quantile)."""
+regrown, a shrunken or an extinct tumour: up to 17% of the replicates end
+with no living cell), and their sample statistics are uncertain well beyond
+a few percent at these sample sizes (the mean of 600 replicates with a
+standard deviation of 108 cells is uncertain by 4.4 cells, 2.2%).  The mean
+therefore matches when it is within 2%, or within 3.3 combined standard
+errors of the two sample means; a quantile when it is within 3% + 2 cells,
+or within 3.3 combined bootstrap standard errors of the two samples'
+quantiles (about a 0.1% two-sided level each)."""
 import sys
 from pathlib import Path
 
@@ -53,7 +56,9 @@ def test_ten_day_distribution_matches_reference_cpu_path(name, params):
     assert all(b.step(i) == md.TEN_DAYS for i in (0, REPLICATES - 1))
     p = stats.ks_2samp(ours, ref).pvalue
     assert p > 0.01, (p, ours.mean(), ref.mean())
-    assert abs(ours.mean() - ref.mean()) <= 0.02 * ref.mean(), (ours.mean(), ref.mean())
+    se_mean = np.hypot(ours.std(ddof=1) / np.sqrt(len(ours)), ref.std(ddof=1) / np.sqrt(len(ref)))
+    tol = max(0.02 * ref.mean(), 3.3 * se_mean)
+    assert abs(ours.mean() - ref.mean()) <= tol, (ours.mean(), ref.mean(), tol)
     for q in (0.1, 0.5, 0.9):
         diff = abs(np.quantile(ours, q) - np.quantile(ref, q))
         tol = max(0.03 * np.quantile(ref, q) + 2, 3.3 * np.hypot(_boot_se(ours, q), _boot_se(ref, q)))
