@@ -304,8 +304,8 @@ struct emt6_batch {
   DevBuf<uint16_t> list;
   DevBuf<int4> meta;
   DevBuf<int32_t> roi, sim_tumor, sim_protocol;
-  DevBuf<uint32_t> step, horizon, counts, err, ticket;
-  DevBuf<int64_t> order;
+  DevBuf<uint32_t> step, horizon, counts, err, ticket, order_hist;
+  DevBuf<int64_t> order;  // per chunk: simulations by region, largest first
   DevBuf<unsigned long long> diffused;
   std::vector<float> h_doses;
 
@@ -405,6 +405,8 @@ struct emt6_batch {
     while (t < target) {
       const uint32_t end = (uint32_t)std::min<uint64_t>(target, (uint64_t)t + chunk);
       if (has_horizon && t >= max_horizon) break;
+      EMT6_CUDA(emt6::launch_order(a, end, order_hist.p, order.p, stream));
+      *count += 3;
       for (int wide = 0; wide < 2; ++wide) {
         int grid = (int)std::min<int64_t>(n, 0x7fffffff);
         if (sched == 1) {
@@ -793,20 +795,10 @@ int emt6_batch_create(const emt6_params *p, const emt6_site *tumors, int32_t n_t
     EMT6_CUDA(b->horizon.alloc((size_t)n_sims));
     EMT6_CUDA(cudaMemcpy(b->horizon.p, sim_horizon, n_sims * 4, cudaMemcpyHostToDevice));
     b->max_horizon = *std::max_element(sim_horizon, sim_horizon + n_sims);
-    // work-queue order: longest horizon first
-    std::vector<int64_t> ord(n_sims);
-    for (int64_t i = 0; i < n_sims; ++i) ord[i] = i;
-    std::stable_sort(ord.begin(), ord.end(), [&](int64_t x, int64_t y) {
-      return sim_horizon[x] > sim_horizon[y];
-    });
-    EMT6_CUDA(b->order.alloc((size_t)n_sims));
-    EMT6_CUDA(cudaMemcpy(b->order.p, ord.data(), n_sims * 8, cudaMemcpyHostToDevice));
-  } else {
-    std::vector<int64_t> ord(n_sims);
-    for (int64_t i = 0; i < n_sims; ++i) ord[i] = i;
-    EMT6_CUDA(b->order.alloc((size_t)n_sims));
-    EMT6_CUDA(cudaMemcpy(b->order.p, ord.data(), n_sims * 8, cudaMemcpyHostToDevice));
   }
+  // launch order, rebuilt on the device before every chunk (emt6::launch_order)
+  EMT6_CUDA(b->order.alloc((size_t)n_sims));
+  EMT6_CUDA(b->order_hist.alloc(emt6::kOrderKeys));
   b->h_doses.assign((size_t)n_protocols * std::max<uint32_t>(protocol_bins, 1), 0.f);
   b->epoch = 0;
   rc = b->reset();

@@ -1116,7 +1116,7 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
       sim = a.order[ticket];
     } else {
       if (item >= a.nsims) break;
-      sim = item;
+      sim = a.order ? a.order[item] : item;
     }
     {
       // nothing to do for a simulation already at its target step
@@ -1374,6 +1374,58 @@ __global__ void __launch_bounds__(WIDE_OK ? 384 : 192, WIDE_OK ? 2 : 4)
 }
 
 // ---------------------------------------------------------------------------
+// launch order: simulations sorted by the region their next step diffuses
+// (largest first), so the CTAs resident on an SM at once mostly run the same
+// diffusion tile code and take similar times.  A counting sort over the
+// region's (rows, columns) key: count, exclusive scan, scatter.  The order
+// inside a key is whatever the atomics give; results do not depend on it
+// (every draw is keyed by the simulation, not by the CTA).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t order_key(const RunArgs &a, int64_t sim, uint32_t t_end) {
+  const uint32_t hz = a.horizon ? a.horizon[sim] : 0xFFFFFFFFu;
+  if (a.step[sim] >= (t_end < hz ? t_end : hz)) return kOrderKeys - 1;  // nothing to do: last
+  const int h = a.roi[sim * 8 + 2], w = a.roi[sim * 8 + 3];
+  const uint32_t nr = (uint32_t)min(h + 2, 63), nc = (uint32_t)min(w + 2, 63);
+  return (kOrderKeys - 2) - (nr * 64u + nc);
+}
+
+__global__ void order_count_kernel(const RunArgs a, uint32_t t_end, uint32_t *hist) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.nsims;
+       i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&hist[order_key(a, i, t_end)], 1u);
+}
+
+__global__ void __launch_bounds__(1024) order_scan_kernel(uint32_t *hist) {
+  // kOrderKeys = 4 x 1024 counters: each thread scans four, then the block
+  __shared__ uint32_t part[1024];
+  const int t = threadIdx.x;
+  uint32_t v[4], run = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = run;
+    run += hist[4 * t + k];
+  }
+  part[t] = run;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const uint32_t add = t >= o ? part[t - o] : 0u;
+    __syncthreads();
+    part[t] += add;
+    __syncthreads();
+  }
+  const uint32_t base = part[t] - run;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) hist[4 * t + k] = base + v[k];
+}
+
+__global__ void order_scatter_kernel(const RunArgs a, uint32_t t_end, uint32_t *hist,
+                                     int64_t *out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.nsims;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[atomicAdd(&hist[order_key(a, i, t_end)], 1u)] = i;
+}
+
+// ---------------------------------------------------------------------------
 // reset: expand the initial tumours into every simulation
 // ---------------------------------------------------------------------------
 __global__ void reset_kernel(const ResetArgs a) {
@@ -1568,6 +1620,19 @@ cudaError_t launch_run(const RunArgs &a, uint32_t t_end, bool wide, int grid,
     run_kernel<true><<<grid, 384, smem, stream>>>(a, t_end);
   else
     run_kernel<false><<<grid, 192, smem, stream>>>(a, t_end);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_order(const RunArgs &a, uint32_t t_end, uint32_t *hist, int64_t *out,
+                         cudaStream_t stream) {
+  if (a.nsims < 1) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(hist, 0, kOrderKeys * sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = (a.nsims + 255) / 256;
+  const int grid = (int)(blocks < 4096 ? blocks : 4096);
+  order_count_kernel<<<grid, 256, 0, stream>>>(a, t_end, hist);
+  order_scan_kernel<<<1, 1024, 0, stream>>>(hist);
+  order_scatter_kernel<<<grid, 256, 0, stream>>>(a, t_end, hist, out);
   return cudaGetLastError();
 }
 

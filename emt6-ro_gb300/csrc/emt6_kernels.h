@@ -32,7 +32,7 @@ struct RunArgs {
   int64_t nsims;
   int queue;  // 1: persistent CTAs take simulations from order[] via *ticket
   uint32_t *ticket;
-  const int64_t *order;
+  const int64_t *order;  // simulation of each CTA or ticket (null: the identity)
 };
 
 struct ResetArgs {
@@ -59,6 +59,11 @@ int max_ctas_per_sm(const KParams &p, bool wide);
 cudaError_t launch_run(const RunArgs &a, uint32_t t_end, bool wide, int grid,
                        cudaStream_t stream);
 cudaError_t launch_reset(const ResetArgs &a, cudaStream_t stream);
+// simulations sorted largest region first into out[0 .. a.nsims) for the
+// launches of a chunk ending at t_end; hist holds kOrderKeys counters
+constexpr uint32_t kOrderKeys = 4096;
+cudaError_t launch_order(const RunArgs &a, uint32_t t_end, uint32_t *hist, int64_t *out,
+                         cudaStream_t stream);
 cudaError_t instr_read(unsigned long long counts[4], double *sum_dp, unsigned long long *hist);
 cudaError_t instr_reset();
 cudaError_t fp32_peak(int device, double *tflops);
