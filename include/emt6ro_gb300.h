@@ -136,8 +136,9 @@ int emt6_batch_launches(emt6_batch *b, unsigned long long *out);
  * FP32 stencil is reported against. No reference counterpart. */
 int emt6_probe_fp32_peak(int32_t device, double *tflops);
 /* Scheduling of emt6_batch_run.  mode bit 0: 0 = one CTA per simulation
- * (default), 1 = persistent CTAs taking simulations from a device work queue
- * ordered longest horizon first; bit 1: capture the run's launch sequence in
+ * (default), 1 = persistent CTAs taking simulations from a device work queue;
+ * either way the simulations are taken largest diffusion region first, in an
+ * order rebuilt on the device before every launch; bit 1: capture the run's launch sequence in
  * a CUDA graph and replay it (re-captured when start step, target, schedule,
  * chunk or epoch change).  steps_per_launch: steps per kernel launch (0 keeps
  * the current value, default 1200). */
