@@ -438,7 +438,9 @@ def run_ours(args, rank, world, dist):
     # ---- roofline of the dominant kernel -------------------------------------
     peak = ctypes.c_double()
     N.check(N.lib().emt6_probe_fp32_peak(dev, ctypes.byref(peak)))
-    kernel_ms = ms_per_step  # both step kernels of a bench step; the wide one has no work
+    # the two step kernels of a bench step together (the narrow one is 96-98% of
+    # it, the launch-order kernels 0.01%): the diffused counter covers both
+    kernel_ms = ms_per_step
     achieved = diffused / args.steps * FLOP_PER_SITE_SUBSTEP / (kernel_ms * 1e-3) / 1e12
     profiles = ROOT / "profiles" / "traffic.json"
     traffic = None
