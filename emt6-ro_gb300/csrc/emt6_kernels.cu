@@ -1385,7 +1385,9 @@ __device__ __forceinline__ uint32_t order_key(const RunArgs &a, int64_t sim, uin
   const uint32_t hz = a.horizon ? a.horizon[sim] : 0xFFFFFFFFu;
   if (a.step[sim] >= (t_end < hz ? t_end : hz)) return kOrderKeys - 1;  // nothing to do: last
   const int h = a.roi[sim * 8 + 2], w = a.roi[sim * 8 + 3];
-  const uint32_t nr = (uint32_t)min(h + 2, 63), nc = (uint32_t)min(w + 2, 63);
+  // regions are at most 56 x 62 (lattice limit); the clamps keep any key in
+  // [0, kOrderKeys - 2] whatever the stored ROI holds
+  const uint32_t nr = (uint32_t)min(max(h + 2, 0), 62), nc = (uint32_t)min(max(w + 2, 0), 63);
   return (kOrderKeys - 2) - (nr * 64u + nc);
 }
 
