@@ -24,7 +24,10 @@
 //   cell update: 8-neighbour vacancy snapshot, Site::step per list entry,
 //     at most one division per simulation (simulation.cu:66-110).
 // Randomness is Philox keyed by (step, simulation, site, occurrence), so the
-// results do not depend on the launch shape.
+// results do not depend on the launch shape, nor on the order in which CTAs
+// take simulations: before every chunk of steps three small kernels sort the
+// simulations by their region, largest first, so that the CTAs resident on
+// an SM run the same tile code (launch_order).
 #include <cuda_runtime.h>
 
 #include <cstdint>
