@@ -1305,6 +1305,29 @@ int emt6_test_diffuse(const emt6_params *p, float *fields, int32_t height, int32
                     device);
 }
 
+int emt6_test_order(const int32_t *roi, const uint32_t *step, const uint32_t *horizon,
+                    int64_t nsims, uint32_t t_end, int64_t *order, int32_t device) {
+  if (!roi || !step || !order || nsims < 1) return fail(EMT6_ERR_INVALID, "null argument");
+  DeviceGuard g(device);
+  EMT6_TMP(int32_t, r, nsims * 8);
+  EMT6_TMP(uint32_t, st, nsims);
+  EMT6_TMP(uint32_t, hz, nsims);
+  EMT6_TMP(uint32_t, hist, emt6::kOrderKeys);
+  EMT6_TMP(int64_t, out, nsims);
+  EMT6_CUDA(cudaMemcpy(r.p, roi, nsims * 8 * sizeof(int32_t), cudaMemcpyHostToDevice));
+  EMT6_CUDA(cudaMemcpy(st.p, step, nsims * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  if (horizon)
+    EMT6_CUDA(cudaMemcpy(hz.p, horizon, nsims * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  emt6::RunArgs a{};
+  a.roi = r.p;
+  a.step = st.p;
+  a.horizon = horizon ? hz.p : nullptr;
+  a.nsims = nsims;
+  EMT6_CUDA(emt6::launch_order(a, t_end, hist.p, out.p, 0));
+  EMT6_CUDA(cudaMemcpy(order, out.p, nsims * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  return EMT6_OK;
+}
+
 }  // extern "C"
 
 namespace emt6 {

@@ -118,6 +118,7 @@ _SIGNATURES = {
     "emt6_test_list": (_c.c_int, [_VP, _c.c_int32, _c.c_int32, _VP, _P(_c.c_uint32), _c.c_int32]),
     "emt6_test_diffuse": (_c.c_int, [_P(Params), _VP, _c.c_int32, _c.c_int32, _VP, _c.c_int32,
                                      _c.c_int32]),
+    "emt6_test_order": (_c.c_int, [_VP, _VP, _VP, _c.c_int64, _c.c_uint32, _VP, _c.c_int32]),
     "emt6_simulate_noalloc": (_c.c_int, [_P(Params), _VP, _c.c_int32, _c.c_int32, _VP, _VP,
                                          _c.c_int64, _VP, _c.c_uint32, _c.c_uint32, _c.c_uint32,
                                          _c.c_uint32, _c.c_uint64, _VP, _VP]),

@@ -207,6 +207,12 @@ int emt6_test_list(const uint8_t *state, int32_t height, int32_t width, uint16_t
 /* variant 0: the narrow kernel's path (regions up to 32 x 31), 1: the wide one */
 int emt6_test_diffuse(const emt6_params *p, float *fields, int32_t height, int32_t width,
                       const int32_t *roi, int32_t variant, int32_t device);
+/* The launch order of a chunk ending at t_end for nsims simulations with
+ * stored ROIs roi[8 i .. 8 i + 4] (r0, c0, h, w, dist), current steps and
+ * optional horizons: order[] receives the simulation indices, largest region
+ * first, simulations with nothing to do last. */
+int emt6_test_order(const int32_t *roi, const uint32_t *step, const uint32_t *horizon,
+                    int64_t nsims, uint32_t t_end, int64_t *order, int32_t device);
 
 /* ---- allocation-free entry point -------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:
