@@ -1400,6 +1400,8 @@ __global__ void order_count_kernel(const RunArgs a, uint32_t t_end, uint32_t *hi
     atomicAdd(&hist[order_key(a, i, t_end)], 1u);
 }
 
+static_assert(kOrderKeys == 4 * 1024, "order_scan_kernel scans four counters per thread");
+
 __global__ void __launch_bounds__(1024) order_scan_kernel(uint32_t *hist) {
   // kOrderKeys = 4 x 1024 counters: each thread scans four, then the block
   __shared__ uint32_t part[1024];
