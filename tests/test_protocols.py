@@ -32,8 +32,9 @@ def test_validate_and_indexing():
     assert P.validate(zero)["indexing"] == "0-indexed"
     odd = [[(5, 1.0), (5, 1.0), (200_000, 1.0)]]
     v = P.validate(odd)
-    assert v["indexing"] == "unaligned" and v["n_repeated_steps"] == 1 and v["n_out_of_range"] == 1
-    assert P.validate([[(0, 1.0)], [(1, 1.0)]])["indexing"] == "mixed"
+    assert v["indexing"] == "unaligned" and v["duplicates_per_protocol"] == 1
+    assert v["n_out_of_range"] == 1 and v["examples_unaligned"] == [5, 5, 200_000]
+    assert P.validate([[(0, 1.0)], [(1, 1.0)]])["indexing"] == "mixed-0-and-1"
     assert P.validate([])["indexing"] == "empty"
 
 
@@ -45,3 +46,46 @@ def test_converted_file_gives_the_same_dose_table(tmp_path):
     loaded = P.to_experiment(P.read_protocols(tmp_path / "tc.txt"))
     assert loaded[0] == sorted(direct[0])
     assert np.array_equal(wl.protocol_doses(loaded, 480), wl.protocol_doses(direct, 480))
+
+
+def _golden():
+    import json
+    from conftest import GOLDEN
+    return GOLDEN, json.loads((GOLDEN / "protocols_ref.json").read_text())
+
+
+def test_tool_outputs_match_the_reference_tool(capsys):
+    """tests/golden/make_protocols.py ran the reference's
+    tools/convert_protocols.py on protocols_in.txt: parsing, the validate
+    report (dict and printed lines), the EMT6-Ro form, its two-line text and
+    the diff against it must be the same here."""
+    from emt6ro import protocols as P
+    G, ref = _golden()
+    parsed = P.read_protocols(G / "protocols_in.txt")
+    assert parsed == [[tuple(e) for e in p] for p in ref["parsed"]]
+    stats = P.validate(parsed)
+    assert stats == ref["validate"]
+    lines = [P.report_line(stats, 300, "protocols_in.txt")]
+    lines.append(f"[protocols_in.txt]   unaligned step examples: {stats['examples_unaligned']}")
+    assert "\n".join(lines) + "\n" == ref["validate_stdout"]
+    emt6 = P.to_experiment(parsed)
+    assert emt6 == [[tuple(e) for e in p] for p in ref["emt6"]]
+    out = []
+    assert P.diff(parsed, emt6, out.append) == ref["diff"]
+    assert "\n".join(out) + "\n" == ref["diff_stdout"]
+
+
+def test_tool_command_line(tmp_path, capsys):
+    import json
+    from emt6ro import protocols as P
+    G, ref = _golden()
+    assert P.main(["validate", str(G / "protocols_in.txt")]) == 1  # off-grid and out of range
+    assert P.main(["to-emt6", str(G / "protocols_in.txt"), "--out", str(tmp_path / "e.json"),
+                   "--canonicalize"]) == 0
+    assert (tmp_path / "e.json").read_text() == json.dumps(ref["emt6"])
+    assert P.main(["to-tumor-ca", str(tmp_path / "e.json"), str(tmp_path / "t.txt")]) == 0
+    assert (tmp_path / "t.txt").read_text() == ref["emt6_two_line"]
+    assert P.main(["diff", str(tmp_path / "t.txt"), str(tmp_path / "e.json")]) == 0
+    assert P.main(["diff", str(G / "protocols_in.txt"), str(tmp_path / "e.json")]) == 1
+    P.write_protocols([[(0, 1.0)]], tmp_path / "ok.txt")
+    assert P.main(["validate", str(tmp_path / "ok.txt")]) == 0
