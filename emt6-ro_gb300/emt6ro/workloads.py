@@ -140,5 +140,7 @@ def protocol_doses(protocols, bins: int, resolution: int = PROTOCOL_RESOLUTION) 
     d = np.zeros((len(protocols), bins), np.float32)
     for i, prot in enumerate(protocols):
         for t, dose in prot:
+            if not 0 <= int(t) // resolution < bins:
+                raise ValueError(f"irradiation step {int(t)} is beyond the protocol length")
             d[i, int(t) // resolution] += np.float32(dose)
     return d
