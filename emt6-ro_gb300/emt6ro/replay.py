@@ -93,16 +93,18 @@ def main(argv=None) -> int:
         protocols = protocols[:args.limit_protocols]
     print(f"{len(protocols)} protocols x {len(tumors)} tumors x {args.reps} reps, "
           f"{args.steps} steps")
+    # a seed drawn here is recorded in the metadata, so the run can be repeated
+    seed = args.seed if args.seed is not None else int.from_bytes(os.urandom(8), "little")
     t0 = time.time()
     counts = replay(params, tumors, protocols, args.reps, args.steps, args.resolution,
-                    args.seed, args.protocol_chunk, args.device, log=print)
+                    seed, args.protocol_chunk, args.device, log=print)
     wall = time.time() - t0
     write_rows(counts, args.out)
     meta.write_text(json.dumps({
         "n_protocols": len(protocols), "n_tumors": len(tumors), "reps_per_tumor": args.reps,
         "steps": args.steps, "resolution": args.resolution,
         "tumors": [str(p) for p in args.tumors], "protocols_file": str(args.protocols),
-        "params_file": str(args.params), "wall_time_sec": wall, "seed": args.seed,
+        "params_file": str(args.params), "wall_time_sec": wall, "seed": seed,
         "row_layout": "values per row are tumor-major then rep-major: "
                       "[t0r0, t0r1, ..., t0r{M-1}, t1r0, ...]"}, indent=2))
     print(f"Total: {len(protocols)} protocols in {wall:.1f}s; wrote {args.out} and {meta}")
