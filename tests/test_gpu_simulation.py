@@ -331,3 +331,21 @@ def test_every_tile_shape_set_bit_exact(params, oracle, layouts):
     ob.run(700, nthreads=4)
     assert (b.counts() == ob.counts()).all()
     _assert_same(b, ob, 4)
+
+
+def test_one_day_bit_exact(params, oracle):
+    """A full simulated day (14,400 steps): tumours of radius 6, 10 and 14
+    under GA-like protocols (doses from hour 2 to hour 20) and none, through
+    growth, irradiation, repair, deaths and regrowth, across the narrow
+    kernel's layouts and into the wide kernel: every site of every simulation
+    bit-identical to the oracle."""
+    from emt6ro import workloads as wl
+    tumors = [wl.disc_tumor(params, r, seed=90 + r) for r in (6, 10, 14)]
+    protocols = [[], [(1200, 2.5), (4800, 2.5), (9000, 2.5), (12000, 2.5)],
+                 [(3000, 1.25), (6600, 1.25)]]
+    st = np.array([0, 1, 2, 0, 1, 2], np.int32)
+    sp = np.array([0, 0, 0, 1, 2, 1], np.int32)
+    b, ob, c, co = _run_pair(params, oracle, tumors, protocols, st, sp, 14_400, seed=1440,
+                             chunks=[600] * 24)
+    assert (c == co).all(), (c, co)
+    _assert_same(b, ob, len(st))
