@@ -3,13 +3,15 @@ one row of final living-cell counts per protocol (tumour-major, then run), the
 layout of the reference's tools/run_protocols_gpu.py and its results files.
 
 The reference's runner builds one Experiment per chunk of 10 protocols.  Here
-the protocols go through persistent batches as large as the device holds
-(`--protocol-chunk` protocols each, by default as many as make about 200,000
-simulations), one index space over the whole file: simulation
-(protocol p, tumour t, run r) is p*T*M + t*M + r, and each batch keys its
-random streams by that global index (emt6_batch_set_index_base), so the
-counts for a seed do not depend on the chunking and equal one Experiment
-over all protocols with that seed.
+the file is one index space: simulation (protocol p, tumour t, run r) is
+g = p*T*M + t*M + r.  It is cut into contiguous ranges of about 200,000
+simulations (`sims_per_batch`), each run as one persistent batch whose random
+streams are keyed by the global index (emt6_batch_set_index_base), so the
+counts for a seed do not depend on the cut and equal one Experiment over all
+protocols with that seed.  With several devices the ranges run in waves, one
+batch per device at a time; under torch.distributed each rank runs the
+contiguous share of the index space of its rank and the counts are gathered
+over the group.
 
     python -m emt6ro.replay --protocols protocols.txt --tumors tumor-*.txt \\
         --params default-parameters.json --reps 100 --steps 144000 --out results.txt
@@ -30,32 +32,56 @@ SIMS_PER_BATCH = 200_000
 
 def replay(params, tumors, protocols, reps: int, steps: int, resolution: int = 300,
            seed: int | None = None, protocol_chunk: int | None = None, device: int = 0,
-           log=None) -> np.ndarray:
-    """Final living counts, shape (protocols, tumours, reps), uint32."""
+           log=None, devices=None, sims_per_batch: int | None = None,
+           process_group=None) -> np.ndarray:
+    """Final living counts, shape (protocols, tumours, reps), uint32.
+
+    protocol_chunk: protocols per batch (the reference runner's knob; sets
+    sims_per_batch to protocol_chunk * T * M).  devices: run batches on these
+    devices concurrently (default [device]).  process_group: a
+    torch.distributed group; every rank returns the whole array."""
     from .batch import Batch
     n_t, n_p = len(tumors), len(protocols)
     per = n_t * reps
-    chunk = protocol_chunk or max(1, SIMS_PER_BATCH // max(per, 1))
+    total = n_p * per
+    if sims_per_batch is None:
+        sims_per_batch = protocol_chunk * per if protocol_chunk else SIMS_PER_BATCH
+    sims_per_batch = max(1, int(sims_per_batch))
     if seed is None:
         seed = int.from_bytes(os.urandom(8), "little")
-    out = np.zeros((n_p, n_t, reps), np.uint32)
-    for p0 in range(0, n_p, chunk):
-        part = protocols[p0:p0 + chunk]
-        n = len(part)
-        t0 = time.time()
-        sim_tumor = np.tile(np.repeat(np.arange(n_t, dtype=np.int32), reps), n)
-        sim_protocol = np.repeat(np.arange(n, dtype=np.int32), per)
-        b = Batch(params, tumors, part, sim_tumor, sim_protocol, protocol_resolution=resolution,
-                  protocol_length=steps, device=device, seed=seed)
-        b.set_index_base(p0 * per)
-        b.run(steps)
-        out[p0:p0 + n] = b.counts().reshape(n, n_t, reps)
-        del b
-        if log:
-            dt = time.time() - t0
-            log(f"  protocols {p0}..{p0 + n - 1} of {n_p}: {n} protocols x {n_t} tumors x "
-                f"{reps} reps in {dt:.1f}s ({n * per / max(dt, 1e-9):.0f} sims/sec)")
-    return out
+    lo, hi = 0, total
+    if process_group is not None:
+        import torch.distributed as dist
+        from .ga_model.sharding import shard_range
+        lo, hi = shard_range(total, dist.get_rank(process_group),
+                             dist.get_world_size(process_group))
+    ranges = [(g0, min(g0 + sims_per_batch, hi)) for g0 in range(lo, hi, sims_per_batch)]
+    devs = list(devices) if devices else [device]
+    local = np.zeros(hi - lo, np.uint32)
+    for w in range(0, len(ranges), len(devs)):
+        live = []
+        for dev, (g0, g1) in zip(devs, ranges[w:w + len(devs)]):
+            g = np.arange(g0, g1)
+            p_first = g0 // per
+            part = protocols[p_first:(g1 - 1) // per + 1]
+            b = Batch(params, tumors, part, ((g % per) // reps).astype(np.int32),
+                      (g // per - p_first).astype(np.int32), protocol_resolution=resolution,
+                      protocol_length=steps, device=dev, seed=seed)
+            b.set_index_base(g0)
+            b.run(steps)  # enqueues; the batches of a wave run concurrently
+            live.append((g0, g1, b, time.time()))
+        for g0, g1, b, t0 in live:
+            local[g0 - lo:g1 - lo] = b.counts()
+            if log:
+                dt = time.time() - t0
+                log(f"  simulations {g0}..{g1 - 1} of {total} (protocols {g0 // per}.."
+                    f"{(g1 - 1) // per}) in {dt:.1f}s ({(g1 - g0) / max(dt, 1e-9):.0f} sims/sec)")
+        live.clear()
+        b = None  # free the wave's batches before the next one is made
+    if process_group is not None:
+        from .ga_model.sharding import gather_shards
+        local = gather_shards(local, total, process_group)
+    return local.reshape(n_p, n_t, reps)
 
 
 def write_rows(counts: np.ndarray, path) -> None:
@@ -78,10 +104,12 @@ def main(argv=None) -> int:
     ap.add_argument("--out", type=Path, required=True)
     ap.add_argument("--meta-out", type=Path, default=None)
     ap.add_argument("--protocol-chunk", type=int, default=None,
-                    help="protocols per batch (default: about 200,000 simulations)")
+                    help="protocols per batch (default: batches of about 200,000 simulations)")
     ap.add_argument("--limit-protocols", type=int, default=None)
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--devices", type=int, nargs="+", default=None,
+                    help="run batches on these devices concurrently")
     args = ap.parse_args(argv)
     args.out.parent.mkdir(parents=True, exist_ok=True)
     meta = args.meta_out or args.out.with_suffix(args.out.suffix + ".meta.json")
@@ -97,7 +125,7 @@ def main(argv=None) -> int:
     seed = args.seed if args.seed is not None else int.from_bytes(os.urandom(8), "little")
     t0 = time.time()
     counts = replay(params, tumors, protocols, args.reps, args.steps, args.resolution,
-                    seed, args.protocol_chunk, args.device, log=print)
+                    seed, args.protocol_chunk, args.device, log=print, devices=args.devices)
     wall = time.time() - t0
     write_rows(counts, args.out)
     meta.write_text(json.dumps({

@@ -83,3 +83,63 @@ def test_results_rows_and_metadata(monkeypatch, tmp_path, params):
     meta = json.loads((tmp_path / "out" / "r.txt.meta.json").read_text())
     assert meta["n_protocols"] == 2 and meta["n_tumors"] == 2 and meta["reps_per_tumor"] == 3
     assert isinstance(meta["seed"], int) and meta["seed"] == _IndexBatch.made[0].kw["seed"]
+
+
+def test_ranges_that_split_protocols_and_device_waves(monkeypatch):
+    import emt6ro.batch
+    from emt6ro import replay as R
+    monkeypatch.setattr(emt6ro.batch, "Batch", _IndexBatch)
+    prots = [[(300 * k, 1.0)] for k in range(5)]
+    for spb in (1, 7, 12, 13, 1000):
+        for devices in (None, [0, 1], [3, 1, 2]):
+            _IndexBatch.made = []
+            out = R.replay(None, ["a", "b", "c"], prots, reps=4, steps=600, seed=2,
+                           sims_per_batch=spb, devices=devices)
+            assert np.array_equal(out.reshape(-1), np.arange(60)), (spb, devices)
+            for b in _IndexBatch.made:
+                g = b.base + np.arange(b.n)
+                first = b.base // 12
+                assert b.protocols == prots[first:(g[-1] // 12) + 1]
+                assert np.array_equal(b.sim_protocol, g // 12 - first)
+                assert np.array_equal(b.sim_tumor, (g % 12) // 4)
+            devs = [b.kw["device"] for b in _IndexBatch.made]
+            want = devices or [0]
+            assert devs == [want[k % len(want)] for k in range(len(devs))]
+
+
+def _gloo_worker(rank, world, port, q):
+    import os
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import emt6ro.batch
+    from emt6ro import replay as R
+    emt6ro.batch.Batch = _IndexBatch
+    prots = [[(300 * k, 1.0)] for k in range(5)]
+    out = R.replay(None, ["a", "b", "c"], prots, reps=4, steps=600, seed=2, sims_per_batch=7,
+                   process_group=dist.group.WORLD)
+    q.put((rank, out.reshape(-1).tolist(), [b.base for b in _IndexBatch.made]))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_replay_over_a_process_group():
+    """World size 2 over gloo: each rank runs its contiguous half of the 60
+    simulations and both get the whole array back."""
+    import multiprocessing as mp
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_gloo_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res[0][1] == list(range(60)) and res[1][1] == list(range(60))
+    assert res[0][2] == [0, 7, 14, 21, 28] and res[1][2] == [30, 37, 44, 51, 58]
