@@ -78,6 +78,14 @@ class EMT6RoModel:
         sim_tumor = ((idx // R) % T).astype(np.int32)
         if seed is None:
             seed = int.from_bytes(os.urandom(8), "little")
+        if process_group is not None:
+            # every rank draws with rank 0's seed: one index space, one seed
+            import torch.distributed as dist
+            box = [int(seed)]
+            dist.broadcast_object_list(box, src=dist.get_global_rank(process_group, 0)
+                                       if hasattr(dist, "get_global_rank") else 0,
+                                       group=process_group)
+            seed = box[0]
         self.seed = int(seed)
         empty = [[] for _ in range(self.num_protocols)]
         self.shards = []

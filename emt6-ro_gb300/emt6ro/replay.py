@@ -38,8 +38,9 @@ def replay(params, tumors, protocols, reps: int, steps: int, resolution: int = 3
 
     protocol_chunk: protocols per batch (the reference runner's knob; sets
     sims_per_batch to protocol_chunk * T * M).  devices: run batches on these
-    devices concurrently (default [device]).  process_group: a
-    torch.distributed group; every rank returns the whole array."""
+    devices concurrently (default [device], this process's GPU).
+    process_group: a torch.distributed group; each rank runs its contiguous
+    share with rank 0's seed and every rank returns the whole array."""
     from .batch import Batch
     n_t, n_p = len(tumors), len(protocols)
     per = n_t * reps
@@ -53,6 +54,12 @@ def replay(params, tumors, protocols, reps: int, steps: int, resolution: int = 3
     if process_group is not None:
         import torch.distributed as dist
         from .ga_model.sharding import shard_range
+        # every rank draws with rank 0's seed: one index space, one seed
+        box = [seed]
+        dist.broadcast_object_list(box, src=dist.get_global_rank(process_group, 0)
+                                   if hasattr(dist, "get_global_rank") else 0,
+                                   group=process_group)
+        seed = box[0]
         lo, hi = shard_range(total, dist.get_rank(process_group),
                              dist.get_world_size(process_group))
     ranges = [(g0, min(g0 + sims_per_batch, hi)) for g0 in range(lo, hi, sims_per_batch)]

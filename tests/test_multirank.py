@@ -128,3 +128,77 @@ def test_shard_range_matches_bench():
         for world in (1, 2, 3, 8):
             assert all(bench.shard_range(total, r, world) == shard_range(total, r, world)
                        for r in range(world))
+
+
+class _FakeShard:
+    """Stands in for a GPU batch: the count of global simulation g is g plus
+    ten times its protocol's total dose; records the seed it was given."""
+
+    def __init__(self, params, tumors, protocols, sim_tumor, sim_protocol, **kw):
+        self.sim_protocol = list(sim_protocol)
+        self.kw, self.base, self.doses = kw, 0, None
+
+    def set_index_base(self, base):
+        self.base = base
+
+    def set_schedule(self, *a):
+        pass
+
+    def add_irradiations(self, protocols):
+        self.doses = [sum(d for _, d in p) for p in protocols]
+
+    def run(self, n):
+        pass
+
+    def counts(self):
+        import numpy as np
+        return np.array([self.base + i + int(10 * self.doses[p])
+                         for i, p in enumerate(self.sim_protocol)], np.uint32)
+
+    def reset(self):
+        self.doses = None
+
+
+_PROTOCOLS = [[(0, 1.0)], [(300, 2.5), (600, 0.5)], [], [(900, 4.0)]]
+
+
+def _model_worker(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import emt6ro.ga_model.model as M
+    M.Batch = _FakeShard
+    m = M.EMT6RoModel(None, ["t0", "t1"], num_protocols=4, num_tests=3,
+                      process_group=dist.group.WORLD)  # seed drawn on rank 0
+    fit = m.predict(_PROTOCOLS)
+    q.put((rank, fit.tolist(), m.seed, [b.kw["seed"] for _, _, b in m.shards]))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_model_over_a_process_group_shares_one_seed_and_gathers():
+    """EMT6RoModel under torch.distributed (world size 2, gloo): both ranks
+    use rank 0's seed, each runs its contiguous shard, and the fitness equals
+    one process holding both shards."""
+    import multiprocessing as mp
+    import emt6ro.ga_model.model as M
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_model_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res[0][1] == res[1][1]
+    assert res[0][2] == res[1][2] and res[0][3] == [res[0][2]] and res[1][3] == [res[0][2]]
+    orig = M.Batch
+    try:
+        M.Batch = _FakeShard
+        one = M.EMT6RoModel(None, ["t0", "t1"], num_protocols=4, num_tests=3, devices=[0, 1],
+                            seed=res[0][2])
+        assert one.predict(_PROTOCOLS).tolist() == res[0][1]
+    finally:
+        M.Batch = orig

@@ -116,9 +116,10 @@ def _gloo_worker(rank, world, port, q):
     from emt6ro import replay as R
     emt6ro.batch.Batch = _IndexBatch
     prots = [[(300 * k, 1.0)] for k in range(5)]
-    out = R.replay(None, ["a", "b", "c"], prots, reps=4, steps=600, seed=2, sims_per_batch=7,
-                   process_group=dist.group.WORLD)
-    q.put((rank, out.reshape(-1).tolist(), [b.base for b in _IndexBatch.made]))
+    out = R.replay(None, ["a", "b", "c"], prots, reps=4, steps=600, sims_per_batch=7,
+                   process_group=dist.group.WORLD)  # seed drawn on rank 0
+    q.put((rank, out.reshape(-1).tolist(), [b.base for b in _IndexBatch.made],
+           {b.kw["seed"] for b in _IndexBatch.made}))
     dist.barrier()
     dist.destroy_process_group()
 
@@ -143,3 +144,4 @@ def test_replay_over_a_process_group():
         assert p.exitcode == 0
     assert res[0][1] == list(range(60)) and res[1][1] == list(range(60))
     assert res[0][2] == [0, 7, 14, 21, 28] and res[1][2] == [30, 37, 44, 51, 58]
+    assert len(res[0][3]) == 1 and res[0][3] == res[1][3]  # one seed on both ranks
